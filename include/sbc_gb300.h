@@ -1,0 +1,160 @@
+/*
+ * sbc_gb300.h -- C-ABI of the GB300 StreamingBC hot path (libsbc_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every function returns SBC_OK (0) or a
+ * negative SBC_ERR_* code; sbc_last_error() gives the calling thread's last
+ * message.  Vertex ids are int64 on the host side (as in the reference) and
+ * must be < 2^31 - 1.
+ *
+ * Objects:
+ *   sbc_graph   device-resident slack-CSR adjacency that accepts insertions in
+ *               place; replaces the STINGER instance (struct stinger,
+ *               src/stinger/stinger.h) of the reference.
+ *   sbc_forest  per-root state of K roots on one graph -- dist int32, sigma
+ *               int64, delta fp64 in [K][V] structure-of-arrays -- plus BC[V];
+ *               replaces bcForest/bcTree (src/streamingbc_aux.h:21-40).
+ * All device work of a graph and its forests runs in order on one CUDA stream
+ * owned by the graph.  Calls on different graphs may run concurrently from
+ * different host threads.
+ */
+#ifndef SBC_GB300_H_
+#define SBC_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SBC_OK 0
+#define SBC_ERR_ARG (-1)         /* bad argument */
+#define SBC_ERR_CUDA (-2)        /* CUDA runtime error (message in sbc_last_error) */
+#define SBC_ERR_NOMEM (-3)       /* device or host allocation failed */
+#define SBC_ERR_STATE (-4)       /* call out of order (e.g. insert before static init) */
+#define SBC_ERR_UNSUPPORTED (-5) /* operation not provided (edge deletion) */
+#define SBC_ERR_NOGPU (-6)       /* no CUDA device */
+
+typedef struct sbc_graph sbc_graph;
+typedef struct sbc_forest sbc_forest;
+
+/* Per-call statistics of an insertion batch (counters match the reference's
+ * COUNT_TRAVERSALS counters, src/streamingbc_internal.c:107-110,203-206,
+ * 365-368,537-540, summed over roots). */
+typedef struct {
+    int64_t inserted;     /* insertions applied */
+    int64_t duplicates;   /* rejected: edge already present */
+    int64_t invalid;      /* rejected: self loop or vertex id out of range */
+    int64_t roots_active; /* roots not culled at batch start */
+    int64_t case1;        /* (insertion, root) pairs with |d| == 1 */
+    int64_t case2;        /* (insertion, root) pairs with |d| > 1 */
+    int64_t vertices;     /* traversed vertices */
+    int64_t edges;        /* traversed edges (sum of degrees of traversed vertices) */
+} sbc_batch_stats;
+
+/* Device time per kernel kind, accumulated while profiling is on. */
+typedef struct {
+    double static_ms;   int64_t static_launches;
+    double append_ms;   int64_t append_launches;
+    double classify_ms; int64_t classify_launches;
+    double update_ms;   int64_t update_launches;
+    double batch_ms;    int64_t batches;
+} sbc_profile;
+
+const char *sbc_last_error(void);
+
+/* Select the CUDA device used by objects created afterwards on this thread. */
+int sbc_set_device(int device);
+
+/* ---- graph -------------------------------------------------------------- */
+
+/* Bulk build from a symmetric CSR (both directions stored), the shape of the
+ * reference's csrGraph (src/streamingbc.h:30-35) fed to CreateStingerFromCSR
+ * (src/sbcMain_utils.c:306-338) / stinger_set_initial_edges
+ * (src/stinger/stinger.c:1142-1282).  off[nv+1], adj[off[nv]]. */
+int sbc_graph_create(sbc_graph **out, int64_t nv, const int64_t *off, const int64_t *adj);
+int sbc_graph_destroy(sbc_graph *g);
+int sbc_graph_num_vertices(const sbc_graph *g, int64_t *nv);
+/* Live degree of v (synchronises the graph's stream).
+ * Replaces stinger_outdegree (src/stinger/stinger.h). */
+int sbc_graph_degree(sbc_graph *g, int64_t v, int64_t *deg);
+/* Directed insertion with stinger_insert_edge's result convention
+ * (src/stinger/stinger.c:778-876): *result = 1 new, 0 already present,
+ * -1 self loop.  Synchronous. */
+int sbc_graph_insert_directed(sbc_graph *g, int64_t from, int64_t to, int *result);
+/* Make room in the adjacency for n future undirected insertions (u[i], v[i])
+ * (host arrays), re-packing the slack CSR if needed.  Needed before
+ * sbc_insert_batch_device, whose endpoints the host cannot see; the host-array
+ * entry points plan capacity themselves.  Synchronous. */
+int sbc_graph_reserve(sbc_graph *g, int64_t n, const int64_t *u, const int64_t *v);
+/* Number of adjacency re-packs so far. */
+int sbc_graph_repacks(const sbc_graph *g, int64_t *count);
+/* Copy the live adjacency back as CSR: off[nv+1]; adj may be NULL to query
+ * off[nv] first.  Neighbour order is storage order. */
+int sbc_graph_to_csr(sbc_graph *g, int64_t *off, int64_t *adj);
+
+/* ---- forest ------------------------------------------------------------- */
+
+/* K roots (roots[K], distinct vertex ids; identity of length NV for exact BC).
+ * Replaces CreateForestApproximate / CreateForestExact
+ * (src/streamingbc_aux.c:103-118, :51-66) plus the per-thread scratch of
+ * createExtraArraysForThreads (src/streamingbc_aux.c:234-296).  `workers`
+ * persistent CTAs are sized from occupancy and free memory (0 = automatic). */
+int sbc_forest_create(sbc_forest **out, sbc_graph *g, int64_t nk, const int64_t *roots, int64_t workers);
+int sbc_forest_destroy(sbc_forest *f);
+/* nv, nk, workers, device bytes held by the forest. */
+int sbc_forest_info(const sbc_forest *f, int64_t *nv, int64_t *nk, int64_t *workers, int64_t *bytes);
+
+/* Static Brandes init over the forest's roots.  Replaces
+ * BrandesApproxCaseParallel / BrandesExactParallel (src/streamingbc_init.c:60-84,
+ * :24-44).  Asynchronous on the graph's stream. */
+int sbc_static_init(sbc_forest *f);
+
+/* Insert n undirected edges (u[i], v[i]) from HOST arrays, in order: each is
+ * appended to the adjacency (both directions) and applied to every root, with
+ * the same result as n calls of stinger_insert_edge x2 + insertEdgeStreamingBC
+ * (src/sbcMain_utils.c:458-471, src/streamingbc.c:88-226).  Duplicates and self
+ * loops are rejected and counted, not applied.  Synchronous; stats may be NULL. */
+int sbc_insert_batch(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, sbc_batch_stats *stats);
+
+/* As sbc_insert_batch, with int32 vertex ids already in DEVICE memory; returns
+ * without synchronising (results are ordered on the graph's stream).  Slack for
+ * these insertions must have been reserved with sbc_graph_reserve; an insertion
+ * that finds no slack is not applied and the next sbc_sync reports it. */
+int sbc_insert_batch_device(sbc_forest *f, int64_t n, const int32_t *d_u, const int32_t *d_v);
+
+/* Apply n insertions whose edges are ALREADY in the adjacency (inserted by
+ * sbc_graph_insert_directed in both directions), exactly like
+ * insertEdgeStreamingBC after the caller's stinger_insert_edge calls.
+ * Synchronous; stats may be NULL. */
+int sbc_update_inserted(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, sbc_batch_stats *stats);
+
+/* Wait for all work queued on the forest's graph stream. */
+int sbc_sync(sbc_forest *f);
+/* Read and reset the traversal/case counters accumulated since the last read. */
+int sbc_read_counters(sbc_forest *f, int64_t *vertices, int64_t *edges, int64_t *case1, int64_t *case2);
+
+/* ---- state read-back (synchronous) ------------------------------------- */
+
+int sbc_get_bc(sbc_forest *f, double *out /* [nv] */);
+/* Rows [r0, r0+nr) of the root-major state; dist uses INT32_MAX for
+ * unreachable, sigma is 0 where unreachable. */
+int sbc_get_dist(sbc_forest *f, int64_t r0, int64_t nr, int32_t *out);
+int sbc_get_sigma(sbc_forest *f, int64_t r0, int64_t nr, int64_t *out);
+int sbc_get_delta(sbc_forest *f, int64_t r0, int64_t nr, double *out);
+
+/* ---- timing -------------------------------------------------------------- */
+
+/* Record CUDA events around every kernel launch of this forest (off by default). */
+int sbc_set_profiling(sbc_forest *f, int on);
+int sbc_get_profile(sbc_forest *f, sbc_profile *out);
+int sbc_reset_profile(sbc_forest *f);
+/* Device-time stopwatch on the forest's stream: sbc_timer_start records an
+ * event; sbc_timer_stop records another, synchronises and returns the ms between. */
+int sbc_timer_start(sbc_forest *f);
+int sbc_timer_stop(sbc_forest *f, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SBC_GB300_H_ */

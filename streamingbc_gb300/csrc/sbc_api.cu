@@ -1,0 +1,1058 @@
+// C-ABI of libsbc_gb300.so: sbc_* entry points (include/sbc_gb300.h), the
+// drop-in streamingbc.h surface of the reference and the STINGER shim.
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/sbc_gb300.h"
+#include "../../include/streamingbc.h"
+#include "sbc_host.h"
+
+namespace {
+
+thread_local std::string t_err;
+thread_local int t_device = -1;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    t_err = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where)
+{
+    return fail(e == cudaErrorMemoryAllocation ? SBC_ERR_NOMEM : SBC_ERR_CUDA, "%s: %s", where,
+                cudaGetErrorString(e));
+}
+
+#define CK(call)                                         \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+template <class T>
+cudaError_t dev_alloc(T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+template <class T>
+void dev_free(T*& p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+int use_device(int dev) { return cudaSetDevice(dev) == cudaSuccess ? SBC_OK : fail(SBC_ERR_CUDA, "cudaSetDevice(%d) failed", dev); }
+
+int current_device()
+{
+    if (t_device >= 0) return t_device;
+    int d = 0;
+    cudaGetDevice(&d);
+    return d;
+}
+
+// Slack policy: room for max(4, deg/8) more neighbours per vertex.
+int32_t slack_cap(int64_t live)
+{
+    int64_t c = live + std::max<int64_t>(4, live / 8);
+    return (int32_t)std::min<int64_t>(c, INT32_MAX - 1);
+}
+
+int ensure_staging(sbc_graph* g, int64_t n)
+{
+    if (n <= g->ins_capacity) return SBC_OK;
+    int cap = (int)std::max<int64_t>(n, 64);
+    if (g->d_ins) cudaFree(g->d_ins);
+    if (g->h_ins) cudaFreeHost(g->h_ins);
+    g->d_ins = nullptr;
+    g->h_ins = nullptr;
+    CK(dev_alloc(&g->d_ins, (size_t)3 * cap));
+    CK(cudaMallocHost((void**)&g->h_ins, sizeof(int32_t) * 3 * (size_t)cap));
+    g->ins_capacity = cap;
+    return SBC_OK;
+}
+
+// Re-pack the adjacency so that every vertex has room for need[v] more slots.
+int repack(sbc_graph* g, const std::unordered_map<int64_t, int64_t>& need)
+{
+    CK(cudaStreamSynchronize(g->stream));
+    std::vector<int32_t> deg(g->nv);
+    if (g->nv) CK(cudaMemcpy(deg.data(), g->d_deg, sizeof(int32_t) * g->nv, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> row(g->nv + 1);
+    std::vector<int32_t> cap(g->nv);
+    int64_t total = 0;
+    for (int64_t v = 0; v < g->nv; ++v) {
+        auto it = need.find(v);
+        int64_t want = deg[v] + (it == need.end() ? 0 : it->second);
+        int32_t c = std::max<int32_t>(g->h_cap[v], slack_cap(want));
+        if (it != need.end()) c = std::max<int32_t>(c, slack_cap(want + want / 4));
+        row[v] = total;
+        cap[v] = c;
+        total += c;
+    }
+    row[g->nv] = total;
+    int64_t* d_row = nullptr;
+    int32_t *d_col = nullptr, *d_seq = nullptr;
+    cudaError_t e;
+    if ((e = dev_alloc(&d_row, g->nv + 1)) || (e = dev_alloc(&d_col, total)) || (e = dev_alloc(&d_seq, total))) {
+        dev_free(d_row);
+        dev_free(d_col);
+        dev_free(d_seq);
+        return cuda_fail(e, "repack allocation");
+    }
+    CK(cudaMemcpyAsync(d_row, row.data(), sizeof(int64_t) * (g->nv + 1), cudaMemcpyHostToDevice, g->stream));
+    CK(sbc::launch_repack(g, d_row, d_col, d_seq));
+    CK(cudaMemcpyAsync(g->d_cap, cap.data(), sizeof(int32_t) * g->nv, cudaMemcpyHostToDevice, g->stream));
+    CK(cudaMemcpyAsync(g->d_deg0, g->d_deg, sizeof(int32_t) * g->nv, cudaMemcpyDeviceToDevice, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    dev_free(g->d_row);
+    dev_free(g->d_col);
+    dev_free(g->d_seq);
+    g->d_row = d_row;
+    g->d_col = d_col;
+    g->d_seq = d_seq;
+    g->total_cap = total;
+    g->h_row = row;
+    g->h_cap = cap;
+    for (int64_t v = 0; v < g->nv; ++v) g->h_deg_ub[v] = deg[v];
+    g->repacks++;
+    return SBC_OK;
+}
+
+// Make sure the n undirected (or directed) insertions fit in the slack;
+// counts them into the host degree upper bound.
+int plan_capacity(sbc_graph* g, int64_t n, const int64_t* u, const int64_t* v, bool directed)
+{
+    std::unordered_map<int64_t, int64_t> need;
+    bool over = false;
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t a = u[i], b = v[i];
+        if (a == b || a < 0 || b < 0 || a >= g->nv || b >= g->nv) continue;
+        int64_t na = ++need[a];
+        if (g->h_deg_ub[a] + na > g->h_cap[a]) over = true;
+        if (!directed) {
+            int64_t nb = ++need[b];
+            if (g->h_deg_ub[b] + nb > g->h_cap[b]) over = true;
+        }
+    }
+    if (over) {
+        int rc = repack(g, need);
+        if (rc) return rc;
+    }
+    for (auto& kv : need) g->h_deg_ub[kv.first] += kv.second;
+    return SBC_OK;
+}
+
+int stage_host(sbc_graph* g, int64_t n, const int64_t* u, const int64_t* v, bool set_ok)
+{
+    int rc = ensure_staging(g, n);
+    if (rc) return rc;
+    const int cap = g->ins_capacity;
+    int32_t* hu = g->h_ins;
+    int32_t* hv = g->h_ins + cap;
+    int32_t* hok = g->h_ins + 2 * cap;
+    for (int64_t i = 0; i < n; ++i) {
+        const bool valid = u[i] >= 0 && v[i] >= 0 && u[i] < g->nv && v[i] < g->nv && u[i] != v[i];
+        hu[i] = valid ? (int32_t)u[i] : 0;
+        hv[i] = valid ? (int32_t)v[i] : 0;
+        hok[i] = valid ? 1 : -1;
+        if (!valid) {
+            // keep ids in range so the append kernel rejects cleanly as a loop
+            hu[i] = -1;
+            hv[i] = -1;
+        }
+    }
+    CK(cudaMemcpyAsync(g->d_ins, hu, sizeof(int32_t) * n, cudaMemcpyHostToDevice, g->stream));
+    CK(cudaMemcpyAsync(g->d_ins + cap, hv, sizeof(int32_t) * n, cudaMemcpyHostToDevice, g->stream));
+    if (set_ok) CK(cudaMemcpyAsync(g->d_ins + 2 * cap, hok, sizeof(int32_t) * n, cudaMemcpyHostToDevice, g->stream));
+    return SBC_OK;
+}
+
+int collect_stats(sbc_forest* f, int64_t n, sbc_batch_stats* st)
+{
+    sbc_graph* g = f->g;
+    if (!st) return SBC_OK;
+    std::vector<int32_t> ok(n);
+    if (n) CK(cudaMemcpyAsync(ok.data(), g->d_ins + 2 * g->ins_capacity, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                              g->stream));
+    int nwork = 0;
+    CK(cudaMemcpyAsync(&nwork, f->d_nwork, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    unsigned long long c[4];
+    CK(cudaMemcpyAsync(c, f->d_counters, sizeof c, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaMemsetAsync(f->d_counters, 0, sizeof c, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    memset(st, 0, sizeof *st);
+    for (int64_t i = 0; i < n; ++i) {
+        if (ok[i] > 0) st->inserted++;
+        else if (ok[i] == 0) st->duplicates++;
+        else st->invalid++;
+    }
+    st->roots_active = nwork;
+    st->vertices = (int64_t)c[0];
+    st->edges = (int64_t)c[1];
+    st->case1 = (int64_t)c[2];
+    st->case2 = (int64_t)c[3];
+    return SBC_OK;
+}
+
+int check_graph_err(sbc_graph* g)
+{
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, g->d_err, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    if (err) {
+        cudaMemsetAsync(g->d_err, 0, sizeof(int), g->stream);
+        return fail(SBC_ERR_STATE, "adjacency slack exhausted during an insertion batch (reserve capacity first)");
+    }
+    return SBC_OK;
+}
+
+template <class T>
+int get_rows(sbc_forest* f, const T* base, int64_t r0, int64_t nr, T* out)
+{
+    if (!f || !out || r0 < 0 || nr < 0 || r0 + nr > f->nk) return fail(SBC_ERR_ARG, "state read: bad row range");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaMemcpyAsync(out, base + (size_t)r0 * f->nv, sizeof(T) * (size_t)nr * f->nv, cudaMemcpyDeviceToHost,
+                       f->g->stream));
+    CK(cudaStreamSynchronize(f->g->stream));
+    return SBC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sbc_last_error(void) { return t_err.c_str(); }
+
+int sbc_set_device(int device)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(SBC_ERR_NOGPU, "no CUDA device");
+    if (device < 0 || device >= n) return fail(SBC_ERR_ARG, "device %d out of range", device);
+    t_device = device;
+    return use_device(device);
+}
+
+// ------------------------------------------------------------------ graph
+
+int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int64_t* adj)
+{
+    if (!out || nv < 0 || nv >= INT32_MAX || !off || (off[nv] > 0 && !adj)) return fail(SBC_ERR_ARG, "sbc_graph_create: bad arguments");
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(SBC_ERR_NOGPU, "no CUDA device");
+    const int dev = current_device();
+    if (use_device(dev)) return SBC_ERR_CUDA;
+    for (int64_t v = 0; v < nv; ++v)
+        if (off[v + 1] < off[v]) return fail(SBC_ERR_ARG, "sbc_graph_create: offsets not monotone at %lld", (long long)v);
+    for (int64_t e = 0; e < off[nv]; ++e)
+        if (adj[e] < 0 || adj[e] >= nv) return fail(SBC_ERR_ARG, "sbc_graph_create: neighbour id out of range at %lld", (long long)e);
+
+    sbc_graph* g = new sbc_graph();
+    g->device = dev;
+    g->nv = nv;
+    g->h_row.resize(nv + 1);
+    g->h_cap.resize(nv);
+    g->h_deg_ub.resize(nv);
+    std::vector<int32_t> deg(nv);
+    int64_t total = 0;
+    for (int64_t v = 0; v < nv; ++v) {
+        const int64_t d = off[v + 1] - off[v];
+        if (d >= INT32_MAX - 8) {
+            delete g;
+            return fail(SBC_ERR_ARG, "degree too large");
+        }
+        deg[v] = (int32_t)d;
+        g->h_row[v] = total;
+        g->h_cap[v] = slack_cap(d);
+        g->h_deg_ub[v] = d;
+        total += g->h_cap[v];
+    }
+    g->h_row[nv] = total;
+    g->total_cap = total;
+    std::vector<int32_t> col(total > 0 ? total : 1, 0);
+    for (int64_t v = 0; v < nv; ++v)
+        for (int64_t e = off[v]; e < off[v + 1]; ++e) col[g->h_row[v] + (e - off[v])] = (int32_t)adj[e];
+
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) || (e = dev_alloc(&g->d_row, nv + 1)) ||
+        (e = dev_alloc(&g->d_deg, nv)) || (e = dev_alloc(&g->d_deg0, nv)) || (e = dev_alloc(&g->d_cap, nv)) ||
+        (e = dev_alloc(&g->d_col, total)) || (e = dev_alloc(&g->d_seq, total)) || (e = dev_alloc(&g->d_err, 1))) {
+        sbc_graph_destroy(g);
+        return cuda_fail(e, "sbc_graph_create allocation");
+    }
+    if ((e = cudaMemcpy(g->d_row, g->h_row.data(), sizeof(int64_t) * (nv + 1), cudaMemcpyHostToDevice)) ||
+        (nv && (e = cudaMemcpy(g->d_deg, deg.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
+        (nv && (e = cudaMemcpy(g->d_deg0, deg.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
+        (nv && (e = cudaMemcpy(g->d_cap, g->h_cap.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
+        (e = cudaMemcpy(g->d_col, col.data(), sizeof(int32_t) * col.size(), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemset(g->d_seq, 0, sizeof(int32_t) * col.size())) || (e = cudaMemset(g->d_err, 0, sizeof(int)))) {
+        sbc_graph_destroy(g);
+        return cuda_fail(e, "sbc_graph_create upload");
+    }
+    int rc = ensure_staging(g, 64);
+    if (rc) {
+        sbc_graph_destroy(g);
+        return rc;
+    }
+    *out = g;
+    return SBC_OK;
+}
+
+int sbc_graph_destroy(sbc_graph* g)
+{
+    if (!g) return SBC_OK;
+    use_device(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    dev_free(g->d_row);
+    dev_free(g->d_deg);
+    dev_free(g->d_deg0);
+    dev_free(g->d_cap);
+    dev_free(g->d_col);
+    dev_free(g->d_seq);
+    dev_free(g->d_err);
+    dev_free(g->d_ins);
+    if (g->h_ins) cudaFreeHost(g->h_ins);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return SBC_OK;
+}
+
+int sbc_graph_num_vertices(const sbc_graph* g, int64_t* nv)
+{
+    if (!g || !nv) return fail(SBC_ERR_ARG, "sbc_graph_num_vertices: null");
+    *nv = g->nv;
+    return SBC_OK;
+}
+
+int sbc_graph_degree(sbc_graph* g, int64_t v, int64_t* deg)
+{
+    if (!g || !deg || v < 0 || v >= g->nv) return fail(SBC_ERR_ARG, "sbc_graph_degree: bad arguments");
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    int32_t d = 0;
+    CK(cudaMemcpyAsync(&d, g->d_deg + v, sizeof d, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    *deg = d;
+    return SBC_OK;
+}
+
+int sbc_graph_insert_directed(sbc_graph* g, int64_t from, int64_t to, int* result)
+{
+    if (!g) return fail(SBC_ERR_ARG, "sbc_graph_insert_directed: null graph");
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    int rc = plan_capacity(g, 1, &from, &to, true);
+    if (rc) return rc;
+    if ((rc = stage_host(g, 1, &from, &to, false))) return rc;
+    CK(sbc::launch_append(g, 1, true));
+    CK(sbc::launch_seal(g, 1));
+    int32_t code = 0;
+    CK(cudaMemcpyAsync(&code, g->d_ins + 2 * g->ins_capacity, sizeof code, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    if (code == -2) return check_graph_err(g);
+    if (result) *result = code < 0 ? -1 : code;
+    return SBC_OK;
+}
+
+int sbc_graph_reserve(sbc_graph* g, int64_t n, const int64_t* u, const int64_t* v)
+{
+    if (!g || n < 0 || (n > 0 && (!u || !v))) return fail(SBC_ERR_ARG, "sbc_graph_reserve: bad arguments");
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    return plan_capacity(g, n, u, v, false);
+}
+
+int sbc_graph_repacks(const sbc_graph* g, int64_t* count)
+{
+    if (!g || !count) return fail(SBC_ERR_ARG, "sbc_graph_repacks: null");
+    *count = g->repacks;
+    return SBC_OK;
+}
+
+int sbc_graph_to_csr(sbc_graph* g, int64_t* off, int64_t* adj)
+{
+    if (!g || !off) return fail(SBC_ERR_ARG, "sbc_graph_to_csr: null");
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    CK(cudaStreamSynchronize(g->stream));
+    std::vector<int32_t> deg(g->nv);
+    if (g->nv) CK(cudaMemcpy(deg.data(), g->d_deg, sizeof(int32_t) * g->nv, cudaMemcpyDeviceToHost));
+    off[0] = 0;
+    for (int64_t v = 0; v < g->nv; ++v) off[v + 1] = off[v] + deg[v];
+    if (!adj) return SBC_OK;
+    std::vector<int32_t> col(g->total_cap > 0 ? g->total_cap : 1);
+    CK(cudaMemcpy(col.data(), g->d_col, sizeof(int32_t) * col.size(), cudaMemcpyDeviceToHost));
+    for (int64_t v = 0; v < g->nv; ++v)
+        for (int32_t s = 0; s < deg[v]; ++s) adj[off[v] + s] = col[g->h_row[v] + s];
+    return SBC_OK;
+}
+
+// ------------------------------------------------------------------ forest
+
+int sbc_forest_create(sbc_forest** out, sbc_graph* g, int64_t nk, const int64_t* roots, int64_t workers)
+{
+    if (!out || !g || nk <= 0 || !roots) return fail(SBC_ERR_ARG, "sbc_forest_create: bad arguments");
+    *out = nullptr;
+    if (nk > g->nv) return fail(SBC_ERR_ARG, "more roots (%lld) than vertices (%lld)", (long long)nk, (long long)g->nv);
+    if (nk >= INT32_MAX) return fail(SBC_ERR_ARG, "too many roots");
+    {
+        std::vector<char> seen(g->nv, 0);
+        for (int64_t r = 0; r < nk; ++r) {
+            if (roots[r] < 0 || roots[r] >= g->nv) return fail(SBC_ERR_ARG, "root %lld out of range", (long long)roots[r]);
+            if (seen[roots[r]]) return fail(SBC_ERR_ARG, "root %lld repeated", (long long)roots[r]);
+            seen[roots[r]] = 1;
+        }
+    }
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    sbc_forest* f = new sbc_forest();
+    f->g = g;
+    f->nv = g->nv;
+    f->nk = nk;
+    f->h_roots.assign(roots, roots + nk);
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, g->device));
+    f->sm_count = prop.multiProcessorCount;
+    const size_t cells = (size_t)nk * (size_t)f->nv;
+    cudaError_t e;
+    if ((e = dev_alloc(&f->d_roots, nk)) || (e = dev_alloc(&f->d_dist, cells)) || (e = dev_alloc(&f->d_sigma, cells)) ||
+        (e = dev_alloc(&f->d_delta, cells)) || (e = dev_alloc(&f->d_bc, f->nv)) || (e = dev_alloc(&f->d_worklist, nk)) ||
+        (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, 4))) {
+        sbc_forest_destroy(f);
+        return cuda_fail(e, "sbc_forest_create state allocation");
+    }
+    f->d_counter = f->d_nwork + 1;
+    f->bytes = (int64_t)(cells * 20 + f->nv * 8);
+
+    // Persistent workers: occupancy-limited, and their scratch (36 B per vertex
+    // each) limited to half of the memory still free.
+    int per_sm = std::min(sbc::update_workers_per_sm(), sbc::static_workers_per_sm());
+    if (per_sm < 1) per_sm = 1;
+    int64_t w = workers > 0 ? workers : (int64_t)per_sm * f->sm_count;
+    const size_t per_worker = (size_t)f->nv * 36 + 16;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    int64_t fit = (int64_t)((free_b / 2) / per_worker);
+    w = std::min<int64_t>(w, std::max<int64_t>(fit, 1));
+    w = std::min<int64_t>(w, nk);
+    w = std::max<int64_t>(w, 1);
+    f->workers = w;
+    const size_t sc = (size_t)w * (size_t)f->nv;
+    if ((e = dev_alloc(&f->d_st, sc)) || (e = dev_alloc(&f->d_dp, sc)) || (e = dev_alloc(&f->d_acc, sc)) ||
+        (e = dev_alloc(&f->d_qd, sc)) || (e = dev_alloc(&f->d_qa, sc)) || (e = dev_alloc(&f->d_qs, sc)) ||
+        (e = dev_alloc(&f->d_lvl, (size_t)w * (size_t)(f->nv + 2)))) {
+        sbc_forest_destroy(f);
+        return cuda_fail(e, "sbc_forest_create scratch allocation");
+    }
+    f->bytes += (int64_t)(sc * 36);
+    CK(cudaMemsetAsync(f->d_st, 0, sizeof(int32_t) * sc, g->stream));
+    CK(cudaMemsetAsync(f->d_dp, 0, sizeof(int64_t) * sc, g->stream));
+    CK(cudaMemsetAsync(f->d_acc, 0, sizeof(double) * sc, g->stream));
+    CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * 4, g->stream));
+    CK(cudaMemcpyAsync(f->d_roots, roots, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, g->stream));
+    for (int k = 0; k < sbc::PROF_COUNT; ++k) {
+        CK(cudaEventCreate(&f->ev_a[k]));
+        CK(cudaEventCreate(&f->ev_b[k]));
+    }
+    CK(cudaEventCreate(&f->t0));
+    CK(cudaEventCreate(&f->t1));
+    CK(cudaStreamSynchronize(g->stream));
+    *out = f;
+    return SBC_OK;
+}
+
+int sbc_forest_destroy(sbc_forest* f)
+{
+    if (!f) return SBC_OK;
+    if (f->g) {
+        use_device(f->g->device);
+        cudaStreamSynchronize(f->g->stream);
+    }
+    dev_free(f->d_roots);
+    dev_free(f->d_dist);
+    dev_free(f->d_sigma);
+    dev_free(f->d_delta);
+    dev_free(f->d_bc);
+    dev_free(f->d_worklist);
+    dev_free(f->d_nwork);
+    dev_free(f->d_counters);
+    dev_free(f->d_st);
+    dev_free(f->d_dp);
+    dev_free(f->d_acc);
+    dev_free(f->d_qd);
+    dev_free(f->d_qa);
+    dev_free(f->d_qs);
+    dev_free(f->d_lvl);
+    for (int k = 0; k < sbc::PROF_COUNT; ++k) {
+        if (f->ev_a[k]) cudaEventDestroy(f->ev_a[k]);
+        if (f->ev_b[k]) cudaEventDestroy(f->ev_b[k]);
+    }
+    if (f->t0) cudaEventDestroy(f->t0);
+    if (f->t1) cudaEventDestroy(f->t1);
+    delete f;
+    return SBC_OK;
+}
+
+int sbc_forest_info(const sbc_forest* f, int64_t* nv, int64_t* nk, int64_t* workers, int64_t* bytes)
+{
+    if (!f) return fail(SBC_ERR_ARG, "sbc_forest_info: null");
+    if (nv) *nv = f->nv;
+    if (nk) *nk = f->nk;
+    if (workers) *workers = f->workers;
+    if (bytes) *bytes = f->bytes;
+    return SBC_OK;
+}
+
+int sbc_static_init(sbc_forest* f)
+{
+    if (!f) return fail(SBC_ERR_ARG, "sbc_static_init: null");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(sbc::launch_static(f));
+    f->initialized = true;
+    return SBC_OK;
+}
+
+int sbc_insert_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, sbc_batch_stats* stats)
+{
+    if (!f || n < 0 || (n > 0 && (!u || !v))) return fail(SBC_ERR_ARG, "sbc_insert_batch: bad arguments");
+    if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_insert_batch before sbc_static_init");
+    if (n >= INT32_MAX) return fail(SBC_ERR_ARG, "batch too large");
+    sbc_graph* g = f->g;
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    if (n == 0) {
+        if (stats) memset(stats, 0, sizeof *stats);
+        return SBC_OK;
+    }
+    int rc = plan_capacity(g, n, u, v, false);
+    if (rc) return rc;
+    if ((rc = stage_host(g, n, u, v, false))) return rc;
+    f->prof_begin(sbc::PROF_BATCH);
+    f->prof_begin(sbc::PROF_APPEND);
+    CK(sbc::launch_append(g, (int)n, false));
+    f->prof_end(sbc::PROF_APPEND);
+    CK(sbc::launch_update(f, (int)n, false));
+    CK(sbc::launch_seal(g, (int)n));
+    f->prof_end(sbc::PROF_BATCH);
+    if ((rc = collect_stats(f, n, stats))) return rc;
+    return check_graph_err(g);
+}
+
+int sbc_insert_batch_device(sbc_forest* f, int64_t n, const int32_t* d_u, const int32_t* d_v)
+{
+    if (!f || n < 0 || (n > 0 && (!d_u || !d_v))) return fail(SBC_ERR_ARG, "sbc_insert_batch_device: bad arguments");
+    if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_insert_batch_device before sbc_static_init");
+    if (n >= INT32_MAX) return fail(SBC_ERR_ARG, "batch too large");
+    if (n == 0) return SBC_OK;
+    sbc_graph* g = f->g;
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    int rc = ensure_staging(g, n);
+    if (rc) return rc;
+    const int cap = g->ins_capacity;
+    f->prof_begin(sbc::PROF_BATCH);
+    CK(cudaMemcpyAsync(g->d_ins, d_u, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, g->stream));
+    CK(cudaMemcpyAsync(g->d_ins + cap, d_v, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, g->stream));
+    f->prof_begin(sbc::PROF_APPEND);
+    CK(sbc::launch_append(g, (int)n, false));
+    f->prof_end(sbc::PROF_APPEND);
+    CK(sbc::launch_update(f, (int)n, false));
+    CK(sbc::launch_seal(g, (int)n));
+    f->prof_end(sbc::PROF_BATCH);
+    return SBC_OK;
+}
+
+int sbc_update_inserted(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, sbc_batch_stats* stats)
+{
+    if (!f || n < 0 || (n > 0 && (!u || !v))) return fail(SBC_ERR_ARG, "sbc_update_inserted: bad arguments");
+    if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_update_inserted before sbc_static_init");
+    sbc_graph* g = f->g;
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    if (n == 0) {
+        if (stats) memset(stats, 0, sizeof *stats);
+        return SBC_OK;
+    }
+    int rc = stage_host(g, n, u, v, true);
+    if (rc) return rc;
+    f->prof_begin(sbc::PROF_BATCH);
+    CK(sbc::launch_update(f, (int)n, true));
+    f->prof_end(sbc::PROF_BATCH);
+    if (stats) return collect_stats(f, n, stats);
+    CK(cudaStreamSynchronize(g->stream));
+    return SBC_OK;
+}
+
+int sbc_sync(sbc_forest* f)
+{
+    if (!f) return fail(SBC_ERR_ARG, "sbc_sync: null");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaStreamSynchronize(f->g->stream));
+    return check_graph_err(f->g);
+}
+
+int sbc_read_counters(sbc_forest* f, int64_t* vertices, int64_t* edges, int64_t* case1, int64_t* case2)
+{
+    if (!f) return fail(SBC_ERR_ARG, "sbc_read_counters: null");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    unsigned long long c[4];
+    CK(cudaMemcpyAsync(c, f->d_counters, sizeof c, cudaMemcpyDeviceToHost, f->g->stream));
+    CK(cudaMemsetAsync(f->d_counters, 0, sizeof c, f->g->stream));
+    CK(cudaStreamSynchronize(f->g->stream));
+    if (vertices) *vertices = (int64_t)c[0];
+    if (edges) *edges = (int64_t)c[1];
+    if (case1) *case1 = (int64_t)c[2];
+    if (case2) *case2 = (int64_t)c[3];
+    return SBC_OK;
+}
+
+int sbc_get_bc(sbc_forest* f, double* out)
+{
+    if (!f || !out) return fail(SBC_ERR_ARG, "sbc_get_bc: null");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaMemcpyAsync(out, f->d_bc, sizeof(double) * f->nv, cudaMemcpyDeviceToHost, f->g->stream));
+    CK(cudaStreamSynchronize(f->g->stream));
+    return SBC_OK;
+}
+
+int sbc_get_dist(sbc_forest* f, int64_t r0, int64_t nr, int32_t* out) { return get_rows(f, f ? f->d_dist : nullptr, r0, nr, out); }
+int sbc_get_sigma(sbc_forest* f, int64_t r0, int64_t nr, int64_t* out) { return get_rows(f, f ? f->d_sigma : nullptr, r0, nr, out); }
+int sbc_get_delta(sbc_forest* f, int64_t r0, int64_t nr, double* out) { return get_rows(f, f ? f->d_delta : nullptr, r0, nr, out); }
+
+int sbc_set_profiling(sbc_forest* f, int on)
+{
+    if (!f) return fail(SBC_ERR_ARG, "sbc_set_profiling: null");
+    f->prof = on != 0;
+    return SBC_OK;
+}
+
+int sbc_get_profile(sbc_forest* f, sbc_profile* out)
+{
+    if (!f || !out) return fail(SBC_ERR_ARG, "sbc_get_profile: null");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    for (int k = 0; k < sbc::PROF_COUNT; ++k) f->prof_collect(k);
+    out->static_ms = f->prof_ms[sbc::PROF_STATIC];
+    out->static_launches = f->prof_n[sbc::PROF_STATIC];
+    out->append_ms = f->prof_ms[sbc::PROF_APPEND];
+    out->append_launches = f->prof_n[sbc::PROF_APPEND];
+    out->classify_ms = f->prof_ms[sbc::PROF_CLASSIFY];
+    out->classify_launches = f->prof_n[sbc::PROF_CLASSIFY];
+    out->update_ms = f->prof_ms[sbc::PROF_UPDATE];
+    out->update_launches = f->prof_n[sbc::PROF_UPDATE];
+    out->batch_ms = f->prof_ms[sbc::PROF_BATCH];
+    out->batches = f->prof_n[sbc::PROF_BATCH];
+    return SBC_OK;
+}
+
+int sbc_reset_profile(sbc_forest* f)
+{
+    if (!f) return fail(SBC_ERR_ARG, "sbc_reset_profile: null");
+    for (int k = 0; k < sbc::PROF_COUNT; ++k) {
+        f->prof_collect(k);
+        f->prof_ms[k] = 0;
+        f->prof_n[k] = 0;
+    }
+    return SBC_OK;
+}
+
+int sbc_timer_start(sbc_forest* f)
+{
+    if (!f) return fail(SBC_ERR_ARG, "sbc_timer_start: null");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaEventRecord(f->t0, f->g->stream));
+    return SBC_OK;
+}
+
+int sbc_timer_stop(sbc_forest* f, double* ms)
+{
+    if (!f || !ms) return fail(SBC_ERR_ARG, "sbc_timer_stop: null");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaEventRecord(f->t1, f->g->stream));
+    CK(cudaEventSynchronize(f->t1));
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, f->t0, f->t1));
+    *ms = t;
+    return SBC_OK;
+}
+
+// ============================================================ STINGER shim
+
+struct stinger {
+    sbc_graph* g;
+};
+
+struct stinger* stinger_new(void)
+{
+    stinger* s = (stinger*)calloc(1, sizeof(stinger));
+    return s;
+}
+
+void stinger_set_initial_edges(struct stinger* G, const size_t nv, const int64_t etype, const int64_t* off,
+                               const int64_t* phys_to, const int64_t* weights, const int64_t* times,
+                               const int64_t* first_times, const int64_t single_ts)
+{
+    (void)etype;
+    (void)weights;
+    (void)times;
+    (void)first_times;
+    (void)single_ts;
+    if (!G) {
+        fail(SBC_ERR_ARG, "stinger_set_initial_edges: null graph");
+        return;
+    }
+    if (G->g) {
+        sbc_graph_destroy(G->g);
+        G->g = nullptr;
+    }
+    sbc_graph_create(&G->g, (int64_t)nv, off, phys_to);
+}
+
+int stinger_insert_edge(struct stinger* G, int64_t type, int64_t from, int64_t to, int64_t weight, int64_t timestamp)
+{
+    (void)type;
+    (void)weight;
+    (void)timestamp;
+    if (!G || !G->g) return -1;
+    int result = -1;
+    if (sbc_graph_insert_directed(G->g, from, to, &result)) return -1;
+    return result;
+}
+
+int stinger_insert_edge_pair(struct stinger* G, int64_t type, int64_t from, int64_t to, int64_t weight,
+                             int64_t timestamp)
+{
+    int a = stinger_insert_edge(G, type, from, to, weight, timestamp);
+    int b = stinger_insert_edge(G, type, to, from, weight, timestamp);
+    if (a < 0 || b < 0) return -1;
+    return a | b;
+}
+
+int stinger_remove_edge(struct stinger* G, int64_t type, int64_t from, int64_t to)
+{
+    (void)G;
+    (void)type;
+    (void)from;
+    (void)to;
+    fail(SBC_ERR_UNSUPPORTED, "stinger_remove_edge: edge deletion is not provided");
+    return -1;
+}
+
+int64_t stinger_outdegree(const struct stinger* G, int64_t v)
+{
+    if (!G || !G->g) return 0;
+    int64_t d = 0;
+    if (sbc_graph_degree(G->g, v, &d)) return 0;
+    return d;
+}
+
+int64_t stinger_typed_outdegree(const struct stinger* G, int64_t v, int64_t type)
+{
+    (void)type;
+    return stinger_outdegree(G, v);
+}
+
+struct stinger* stinger_free(struct stinger* G)
+{
+    if (G) {
+        sbc_graph_destroy(G->g);
+        free(G);
+    }
+    return nullptr;
+}
+
+struct sbc_graph* stinger_sbc_graph(struct stinger* G) { return G ? G->g : nullptr; }
+
+// ======================================================= streamingbc.h surface
+
+static bcForest* make_host_forest(int64_t NV, int64_t NK, const int64_t* roots)
+{
+    bcForest* f = (bcForest*)calloc(1, sizeof(bcForest));
+    if (!f) return nullptr;
+    f->NV = NV;
+    f->forest = (bcTreePtr*)calloc((size_t)(NV > 0 ? NV : 1), sizeof(bcTreePtr));
+    f->totalBC = (bc_t*)calloc((size_t)(NV > 0 ? NV : 1), sizeof(bc_t));
+    f->sbc_nk = NK;
+    f->sbc_roots = (int64_t*)malloc(sizeof(int64_t) * (size_t)(NK > 0 ? NK : 1));
+    if (!f->forest || !f->totalBC || !f->sbc_roots) {
+        free(f->forest);
+        free(f->totalBC);
+        free(f->sbc_roots);
+        free(f);
+        return nullptr;
+    }
+    for (int64_t r = 0; r < NK; ++r) f->sbc_roots[r] = roots ? roots[r] : r;
+    return f;
+}
+
+bcForest* streamingBCCreateForestExact(int64_t NV) { return make_host_forest(NV, NV, nullptr); }
+
+bcForest* streamingBCCreateForestApproximate(int64_t NV, int64_t NK, int64_t* rootArrayForApproximation)
+{
+    if (NK > NV || NK < 0 || !rootArrayForApproximation) {
+        fail(SBC_ERR_ARG, "streamingBCCreateForestApproximate: bad arguments");
+        return nullptr;
+    }
+    return make_host_forest(NV, NK, rootArrayForApproximation);
+}
+
+static void free_host_forest(bcForestPtr* dead)
+{
+    if (!dead || !*dead) return;
+    bcForest* f = *dead;
+    for (int64_t v = 0; v < f->NV; ++v)
+        if (f->forest[v]) {
+            free(f->forest[v]->vArr);
+            free(f->forest[v]);
+        }
+    sbc_forest_destroy(f->sbc);
+    free(f->forest);
+    free(f->totalBC);
+    free(f->sbc_roots);
+    free(f);
+    *dead = nullptr;
+}
+
+void streamingBCDeleteForestExact(bcForestPtr* deadForest) { free_host_forest(deadForest); }
+
+void streamingBCDeleteForestApproximate(bcForestPtr* deadForest, int64_t rootArraySize, int64_t* rootArray)
+{
+    (void)rootArraySize;
+    (void)rootArray;
+    free_host_forest(deadForest);
+}
+
+extraArraysPerThread** streamingBCCreateAuxilary(int64_t threadCount, int64_t NV)
+{
+    (void)NV;
+    if (threadCount < 1) threadCount = 1;
+    extraArraysPerThread** a = (extraArraysPerThread**)calloc((size_t)threadCount, sizeof(extraArraysPerThread*));
+    if (!a) return nullptr;
+    for (int64_t t = 0; t < threadCount; ++t) a[t] = (extraArraysPerThread*)calloc(1, sizeof(extraArraysPerThread));
+    return a;
+}
+
+void streamingBCDeleteAuxilary(extraArraysPerThread** parallelExtra, int64_t threadCount, int64_t NV)
+{
+    (void)NV;
+    if (!parallelExtra) return;
+    for (int64_t t = 0; t < threadCount; ++t) free(parallelExtra[t]);
+    free(parallelExtra);
+}
+
+void ClearCounters(extraArraysPerThread* eapt)
+{
+    if (eapt) memset(eapt, 0, sizeof *eapt);
+}
+
+static int refresh_bc(bcForest* forest) { return sbc_get_bc(forest->sbc, forest->totalBC); }
+
+static void static_common(bcForest* forest, struct stinger* G, extraArraysPerThread** aux)
+{
+    if (!forest || !G || !G->g) {
+        fail(SBC_ERR_ARG, "streamingBCInitStatic: forest or graph missing");
+        return;
+    }
+    if (forest->sbc && forest->sbc->g != G->g) {
+        sbc_forest_destroy(forest->sbc);
+        forest->sbc = nullptr;
+    }
+    if (!forest->sbc && sbc_forest_create(&forest->sbc, G->g, forest->sbc_nk, forest->sbc_roots, 0)) return;
+    if (sbc_static_init(forest->sbc)) return;
+    int64_t vtx = 0, edg = 0;
+    if (sbc_read_counters(forest->sbc, &vtx, &edg, nullptr, nullptr)) return;
+    if (aux && aux[0]) {
+        aux[0]->staticTraverseVerticeCounter += vtx;
+        aux[0]->staticTraverseEdgeCounter += edg;
+    }
+    refresh_bc(forest);
+}
+
+void streamingBCInitStaticExact(bcForest* forest, struct stinger* stingerGraph, int64_t NT,
+                                extraArraysPerThread** auxilary)
+{
+    (void)NT;
+    static_common(forest, stingerGraph, auxilary);
+}
+
+void streamingBCInitStaticApproximate(bcForest* forest, struct stinger* stingerGraph, int64_t NT,
+                                      extraArraysPerThread** auxilary, int64_t NK, int64_t* rootArrayForApproximation)
+{
+    (void)NT;
+    if (forest && rootArrayForApproximation && NK == forest->sbc_nk)
+        memcpy(forest->sbc_roots, rootArrayForApproximation, sizeof(int64_t) * (size_t)NK);
+    static_common(forest, stingerGraph, auxilary);
+}
+
+StreamingExtraInfo insertEdgeStreamingBC(bcForest* forest, struct stinger* sStinger, int64_t newU, int64_t newV,
+                                         int64_t* rootArrayForApproximation, int64_t NK, int64_t NV, int64_t NT,
+                                         extraArraysPerThread** eAPT, uint32_t loadBalancing, uint32_t granularity)
+{
+    (void)rootArrayForApproximation;
+    (void)NV;
+    (void)NT;
+    (void)loadBalancing;
+    (void)granularity;
+    StreamingExtraInfo sei = {0, 0, 0, 0};
+    if (!forest || !forest->sbc || !sStinger || forest->sbc->g != sStinger->g) {
+        fail(SBC_ERR_STATE, "insertEdgeStreamingBC: static init on this graph has not run");
+        return sei;
+    }
+    sbc_batch_stats st;
+    if (sbc_update_inserted(forest->sbc, 1, &newU, &newV, &st)) return sei;
+    sei.adjacent = st.case1;
+    sei.movement = st.case2;
+    sei.sameLevel = NK - st.case1 - st.case2;
+    if (eAPT && eAPT[0]) {
+        eAPT[0]->adjacentCounter += st.case1;
+        eAPT[0]->movementCounter += st.case2;
+        eAPT[0]->dynamicTraverseVerticeCounter += st.vertices;
+        eAPT[0]->dynamicTraverseEdgeCounter += st.edges;
+    }
+    refresh_bc(forest);
+    return sei;
+}
+
+StreamingExtraInfo deleteEdgeStreamingBC(bcForest* forest, struct stinger* sStinger, int64_t oldU, int64_t oldV,
+                                         int64_t* rootArrayForApproximation, int64_t NK, int64_t Nv, int64_t NT,
+                                         extraArraysPerThread** eAPT, uint32_t loadBalancing, uint32_t granularity)
+{
+    (void)forest; (void)sStinger; (void)oldU; (void)oldV; (void)rootArrayForApproximation; (void)NK;
+    (void)Nv; (void)NT; (void)eAPT; (void)loadBalancing; (void)granularity;
+    fail(SBC_ERR_UNSUPPORTED, "deleteEdgeStreamingBC: edge deletion is not provided");
+    StreamingExtraInfo sei = {0, 0, 0, 0};
+    return sei;
+}
+
+// src/streamingbc.c:56-77: insert every edge of the new vertex, one at a time.
+StreamingExtraInfo insertVertexStreamingBC(bcForest* forest, struct stinger* sStinger, int64_t src,
+                                           int64_t* adjacencyArray, int64_t adjacencySize,
+                                           int64_t* rootArrayForApproximation, int64_t NK, int64_t NV, int64_t NT,
+                                           extraArraysPerThread** eAPT)
+{
+    StreamingExtraInfo total = {0, 0, 0, 0};
+    for (int64_t d = 0; d < adjacencySize; ++d) {
+        const int64_t dest = adjacencyArray[d];
+        stinger_insert_edge(sStinger, 0, src, dest, 0, 0);
+        stinger_insert_edge(sStinger, 0, dest, src, 0, 0);
+        StreamingExtraInfo one = insertEdgeStreamingBC(forest, sStinger, src, dest, rootArrayForApproximation, NK, NV,
+                                                       NT, eAPT, BALANCE, FINE);
+        total.adjacent += one.adjacent;
+        total.movement += one.movement;
+        total.sameLevel += one.sameLevel;
+    }
+    return total;
+}
+
+StreamingExtraInfo deleteVertexStreamingBC(bcForest* forest, struct stinger* sStinger, int64_t src,
+                                           int64_t* adjacencyArray, int64_t* adjacencySize,
+                                           int64_t* rootArrayForApproximation, int64_t NK, int64_t NV, int64_t NT,
+                                           extraArraysPerThread** eAPT)
+{
+    (void)forest; (void)sStinger; (void)src; (void)adjacencyArray; (void)rootArrayForApproximation;
+    (void)NK; (void)NV; (void)NT; (void)eAPT;
+    if (adjacencySize) *adjacencySize = 0;
+    fail(SBC_ERR_UNSUPPORTED, "deleteVertexStreamingBC: edge deletion is not provided");
+    StreamingExtraInfo sei = {0, 0, 0, 0};
+    return sei;
+}
+
+int streamingBCSyncForest(bcForest* forest)
+{
+    if (!forest || !forest->sbc) return fail(SBC_ERR_STATE, "streamingBCSyncForest: no device forest");
+    sbc_forest* f = forest->sbc;
+    const int64_t nv = forest->NV;
+    std::vector<int32_t> dist(nv);
+    std::vector<int64_t> sig(nv);
+    std::vector<double> del(nv);
+    for (int64_t r = 0; r < f->nk; ++r) {
+        int rc;
+        if ((rc = sbc_get_dist(f, r, 1, dist.data())) || (rc = sbc_get_sigma(f, r, 1, sig.data())) ||
+            (rc = sbc_get_delta(f, r, 1, del.data())))
+            return rc;
+        const int64_t root = f->h_roots[r];
+        bcTree* t = forest->forest[root];
+        if (!t) {
+            t = (bcTree*)calloc(1, sizeof(bcTree));
+            if (!t) return fail(SBC_ERR_NOMEM, "streamingBCSyncForest: host allocation");
+            t->NV = nv;
+            t->vArr = (bcV*)calloc((size_t)(nv > 0 ? nv : 1), sizeof(bcV));
+            if (!t->vArr) {
+                free(t);
+                return fail(SBC_ERR_NOMEM, "streamingBCSyncForest: host allocation");
+            }
+            forest->forest[root] = t;
+        }
+        for (int64_t x = 0; x < nv; ++x) {
+            const bool reach = dist[x] != SBC_INF;
+            t->vArr[x].level = reach ? dist[x] : INT64_MAX;
+            t->vArr[x].sigma = reach ? sig[x] : INT64_MAX;
+            t->vArr[x].delta = del[x];
+            t->vArr[x].edgesAbove = 0;
+            t->vArr[x].edgesBelow = 0;
+        }
+    }
+    return refresh_bc(forest);
+}
+
+// ---- CSR helpers of the reference driver (src/sbcMain_utils.c:306-362, :425-456)
+
+void CreateStingerFromCSR(csrGraph* csr, struct stinger** stingerGraph)
+{
+    if (!csr || !stingerGraph) return;
+    *stingerGraph = stinger_new();
+    stinger_set_initial_edges(*stingerGraph, (size_t)csr->NV, 0, csr->vertexPointerArray, csr->edgeArray, nullptr,
+                              nullptr, nullptr, 0);
+}
+
+static csrGraph* empty_csr(int64_t NV, int64_t NE)
+{
+    csrGraph* g = (csrGraph*)malloc(sizeof(csrGraph));
+    if (!g) return nullptr;
+    g->NV = NV;
+    g->NE = NE;
+    g->vertexPointerArray = (int64_t*)calloc((size_t)NV + 1, sizeof(int64_t));
+    g->edgeArray = (int64_t*)malloc(sizeof(int64_t) * (size_t)(NE > 0 ? NE : 1));
+    return g;
+}
+
+csrGraph* CreateEmptyUndirectedCSR(int64_t NV, int64_t NE) { return empty_csr(NV, NE * 2); }
+csrGraph* CreateEmptyDirectedCSR(int64_t NV, int64_t NE) { return empty_csr(NV, NE); }
+
+void FreeCSR(csrGraph* graph)
+{
+    if (!graph) return;
+    free(graph->vertexPointerArray);
+    free(graph->edgeArray);
+    free(graph);
+}
+
+void PickRoots(int64_t* rootArrayForApproximation, int64_t NK, int64_t NV)
+{
+    if (NK == NV) {
+        for (int64_t r = 0; r < NK; ++r) rootArrayForApproximation[r] = r;
+        return;
+    }
+    if (NK > NV) {
+        fail(SBC_ERR_ARG, "PickRoots: number of roots is greater than number of vertices");
+        return;
+    }
+    std::vector<char> flag(NV, 0);
+    for (int64_t r = 0; r < NK; ++r) {
+        int64_t v = rand() % NV;
+        if (flag[v]) {
+            --r;
+            continue;
+        }
+        rootArrayForApproximation[r] = v;
+        flag[v] = 1;
+    }
+}
+
+}  // extern "C"

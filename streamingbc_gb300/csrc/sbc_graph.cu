@@ -1,0 +1,118 @@
+// Device slack-CSR adjacency: in-place insertion and re-pack.
+//
+// Replaces stinger_insert_edge (src/stinger/stinger.c:778-876) and the edge
+// block pool.  Each vertex owns slots [row[v], row[v]+cap[v]); the first deg[v]
+// hold live neighbours.  An insertion appends into the slack of both endpoints
+// (one direction for the directed form) after a duplicate check, and stamps the
+// slot with the insertion's index inside its batch (seq), so that a traversal
+// for insertion i of a batch sees only edges of insertions <= i.
+#include "sbc_host.h"
+#include "sbc_internal.cuh"
+
+namespace sbc {
+
+// Insertion outcome codes written to ok[i]:
+//   1 inserted, 0 duplicate (edge already present), -1 self loop or id out of
+//   range, -2 no slack left (the host plans capacity so this is not expected).
+__global__ void k_append(int64_t nv, const int64_t* __restrict__ row, int32_t* deg, const int32_t* __restrict__ cap,
+                         int32_t* col, int32_t* seq, int n, const int32_t* __restrict__ iu,
+                         const int32_t* __restrict__ iv, int32_t* ok, int directed, int* err)
+{
+    const int lane = threadIdx.x;
+    for (int i = 0; i < n; ++i) {
+        const int u = iu[i], v = iv[i];
+        int code = 1;
+        if (u == v || u < 0 || v < 0 || u >= nv || v >= nv) code = -1;
+        if (code == 1) {
+            int x = u, y = v;
+            if (!directed && deg[v] < deg[u]) {
+                x = v;
+                y = u;
+            }
+            const int dx = deg[x];
+            const int64_t rx = row[x];
+            bool found = false;
+            for (int s = lane; s < dx; s += 32)
+                if (col[rx + s] == y) found = true;
+            if (__any_sync(0xffffffffu, found)) code = 0;
+        }
+        if (code == 1 && !(deg[u] < cap[u] && (directed || deg[v] < cap[v]))) {
+            code = -2;
+            if (lane == 0) atomicExch(err, 1);
+        }
+        if (lane == 0) {
+            if (code == 1) {
+                int p = deg[u];
+                col[row[u] + p] = v;
+                seq[row[u] + p] = i;
+                deg[u] = p + 1;
+                if (!directed) {
+                    p = deg[v];
+                    col[row[v] + p] = u;
+                    seq[row[v] + p] = i;
+                    deg[v] = p + 1;
+                }
+            }
+            ok[i] = code;
+        }
+        __syncwarp();
+    }
+}
+
+// After a batch: every appended slot becomes visible to all later traversals.
+__global__ void k_seal(int n, const int32_t* __restrict__ iu, const int32_t* __restrict__ iv,
+                       const int32_t* __restrict__ ok, const int32_t* __restrict__ deg, int32_t* deg0)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || ok[i] <= 0) return;
+    deg0[iu[i]] = deg[iu[i]];
+    deg0[iv[i]] = deg[iv[i]];
+}
+
+// Copy every vertex's live slots to a new layout with larger slack (warp per vertex).
+__global__ void k_repack(int64_t nv, const int64_t* __restrict__ orow, const int32_t* __restrict__ deg,
+                         const int32_t* __restrict__ ocol, const int32_t* __restrict__ oseq,
+                         const int64_t* __restrict__ nrow, int32_t* __restrict__ ncol, int32_t* __restrict__ nseq)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < nv; v += nwarps) {
+        const int d = deg[v];
+        const int64_t a = orow[v], b = nrow[v];
+        for (int s = lane; s < d; s += 32) {
+            ncol[b + s] = ocol[a + s];
+            nseq[b + s] = oseq[a + s];
+        }
+    }
+}
+
+cudaError_t launch_append(sbc_graph* g, int n, bool directed)
+{
+    const int32_t* iu = g->d_ins;
+    const int32_t* iv = g->d_ins + g->ins_capacity;
+    int32_t* ok = g->d_ins + 2 * g->ins_capacity;
+    k_append<<<1, 32, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_cap, g->d_col, g->d_seq, n, iu, iv, ok,
+                                      directed ? 1 : 0, g->d_err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seal(sbc_graph* g, int n)
+{
+    const int32_t* iu = g->d_ins;
+    const int32_t* iv = g->d_ins + g->ins_capacity;
+    const int32_t* ok = g->d_ins + 2 * g->ins_capacity;
+    k_seal<<<(n + 255) / 256, 256, 0, g->stream>>>(n, iu, iv, ok, g->d_deg, g->d_deg0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq)
+{
+    int64_t blocks = (g->nv * 32 + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    if (blocks < 1) blocks = 1;
+    k_repack<<<(int)blocks, 256, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_col, g->d_seq, d_new_row, d_new_col,
+                                                 d_new_seq);
+    return cudaGetLastError();
+}
+
+}  // namespace sbc

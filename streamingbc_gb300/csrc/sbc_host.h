@@ -1,0 +1,134 @@
+// Host-side objects behind the C-ABI (include/sbc_gb300.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+#include "sbc_internal.cuh"
+
+namespace sbc {
+
+enum ProfKernel { PROF_STATIC = 0, PROF_APPEND, PROF_CLASSIFY, PROF_UPDATE, PROF_BATCH, PROF_COUNT };
+
+}  // namespace sbc
+
+// Device-resident slack-CSR adjacency (replaces the STINGER edge-block store,
+// src/stinger/stinger-internal.h:45-103).  All device work for the graph and
+// for forests bound to it runs on `stream`, in order.
+struct sbc_graph {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int64_t nv = 0;
+    int64_t total_cap = 0;
+    int64_t* d_row = nullptr;
+    int32_t* d_deg = nullptr;
+    int32_t* d_deg0 = nullptr;
+    int32_t* d_cap = nullptr;
+    int32_t* d_col = nullptr;
+    int32_t* d_seq = nullptr;
+    int* d_err = nullptr;
+    // host mirrors used to plan re-packs without reading the device
+    std::vector<int64_t> h_row;
+    std::vector<int32_t> h_cap;
+    std::vector<int64_t> h_deg_ub;  // upper bound of the live degree
+    // staging for insertion batches
+    int ins_capacity = 0;
+    int32_t* d_ins = nullptr;  // [3 * ins_capacity]: u, v, ok
+    int32_t* h_ins = nullptr;  // pinned [2 * ins_capacity]
+    int64_t repacks = 0;
+
+    sbc::DevGraph dev() const
+    {
+        sbc::DevGraph G;
+        G.nv = nv;
+        G.row = d_row;
+        G.deg = d_deg;
+        G.deg0 = d_deg0;
+        G.col = d_col;
+        G.seq = d_seq;
+        return G;
+    }
+};
+
+struct sbc_forest {
+    sbc_graph* g = nullptr;
+    int64_t nv = 0, nk = 0;
+    std::vector<int64_t> h_roots;
+    int64_t* d_roots = nullptr;
+    int32_t* d_dist = nullptr;
+    int64_t* d_sigma = nullptr;
+    double* d_delta = nullptr;
+    double* d_bc = nullptr;
+    bool initialized = false;
+    // persistent workers and their scratch
+    int sm_count = 0;
+    int64_t workers = 0;
+    int32_t* d_st = nullptr;
+    int64_t* d_dp = nullptr;
+    double* d_acc = nullptr;
+    int32_t* d_qd = nullptr;
+    int32_t* d_qa = nullptr;
+    int32_t* d_qs = nullptr;
+    int32_t* d_lvl = nullptr;
+    int* d_worklist = nullptr;
+    int* d_nwork = nullptr;   // [1]
+    int* d_counter = nullptr; // [1]
+    unsigned long long* d_counters = nullptr;  // [4]: vertices, edges, case1, case2
+    int64_t bytes = 0;
+    // profiling: CUDA events around each kernel kind
+    bool prof = false;
+    cudaEvent_t ev_a[sbc::PROF_COUNT] = {};
+    cudaEvent_t ev_b[sbc::PROF_COUNT] = {};
+    bool ev_pending[sbc::PROF_COUNT] = {};
+    double prof_ms[sbc::PROF_COUNT] = {};
+    int64_t prof_n[sbc::PROF_COUNT] = {};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+
+    sbc::ScratchBase scratch() const
+    {
+        sbc::ScratchBase s;
+        s.st = d_st;
+        s.dp = d_dp;
+        s.acc = d_acc;
+        s.qd = d_qd;
+        s.qa = d_qa;
+        s.qs = d_qs;
+        s.lvl = d_lvl;
+        return s;
+    }
+    void prof_collect(int k)
+    {
+        if (ev_pending[k]) {
+            float ms = 0.f;
+            cudaEventSynchronize(ev_b[k]);
+            cudaEventElapsedTime(&ms, ev_a[k], ev_b[k]);
+            prof_ms[k] += ms;
+            prof_n[k] += 1;
+            ev_pending[k] = false;
+        }
+    }
+    void prof_begin(int k)
+    {
+        if (!prof) return;
+        prof_collect(k);
+        cudaEventRecord(ev_a[k], g->stream);
+    }
+    void prof_end(int k)
+    {
+        if (!prof) return;
+        cudaEventRecord(ev_b[k], g->stream);
+        ev_pending[k] = true;
+    }
+};
+
+namespace sbc {
+int static_workers_per_sm();
+int update_workers_per_sm();
+cudaError_t launch_static(sbc_forest* f);
+// Classify + cull + update for insertions already staged in g->d_ins
+// (u, v, ok rows).  `all_visible` ignores the per-slot sequence numbers.
+cudaError_t launch_update(sbc_forest* f, int n, bool all_visible);
+cudaError_t launch_append(sbc_graph* g, int n, bool directed);
+cudaError_t launch_seal(sbc_graph* g, int n);
+cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq);
+}  // namespace sbc

@@ -1,0 +1,177 @@
+// Internal device-side definitions of the GB300 StreamingBC hot path.
+//
+// HBM layout (one graph, one forest):
+//   adjacency  slack CSR: row[v] (int64 slot start), deg[v] live degree, cap[v],
+//              deg0[v] degree when the current batch began, col[slot] int32
+//              neighbour id, seq[slot] int32 global insertion sequence number of
+//              slots appended by insertions (read only for slots >= deg0[v]).
+//   forest     structure-of-arrays, root-major: dist[K][V] int32
+//              (SBC_INF = unreachable), sigma[K][V] int64 (0 when unreachable),
+//              delta[K][V] fp64, bc[V] fp64.
+//   workers    per persistent-CTA scratch, V entries each: st int32 (state bits),
+//              dp int64 (diffPath), acc fp64 (dependency accumulator), and three
+//              int32 vertex queues (descent, ascent-up, ascent-same) plus level
+//              offsets.  Scratch is reset in O(touched) after every job.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define SBC_INF 0x7fffffff
+
+// Worker state bits (st[]).  Low bits: descent step + 1 (0 = not a descent
+// vertex).  MOVED: the vertex moved up a level.  ASC: touched by the ascent only.
+#define SBC_STEP_MASK 0x03ffffff
+#define SBC_MOVED 0x08000000
+#define SBC_ASC 0x10000000
+
+namespace sbc {
+
+struct DevGraph {
+    int64_t nv;
+    const int64_t* row;
+    const int32_t* deg;
+    const int32_t* deg0;
+    const int32_t* col;
+    const int32_t* seq;
+};
+
+struct Scratch {
+    int32_t* st;
+    int64_t* dp;
+    double* acc;
+    int32_t* qd;
+    int32_t* qa;
+    int32_t* qs;
+    int32_t* lvl;
+};
+
+// Slots of one worker w inside the worker-major scratch arrays.
+struct ScratchBase {
+    int32_t* st;
+    int64_t* dp;
+    double* acc;
+    int32_t* qd;
+    int32_t* qa;
+    int32_t* qs;
+    int32_t* lvl;  // (nv + 2) per worker
+    __device__ __forceinline__ Scratch of(int w, int64_t nv) const
+    {
+        Scratch s;
+        size_t o = (size_t)w * (size_t)nv;
+        s.st = st + o;
+        s.dp = dp + o;
+        s.acc = acc + o;
+        s.qd = qd + o;
+        s.qa = qa + o;
+        s.qs = qs + o;
+        s.lvl = lvl + (size_t)w * (size_t)(nv + 2);
+        return s;
+    }
+};
+
+// Number of neighbour slots of x visible to the insertion with sequence g:
+// every slot below deg0[x], then appended slots while their seq <= g (slots are
+// appended in sequence order).
+__device__ __forceinline__ int vis_deg(const DevGraph& G, int x, int64_t rs, int g)
+{
+    int d0 = G.deg0[x];
+    int d = G.deg[x];
+    while (d0 < d && G.seq[rs + d0] <= g) ++d0;
+    return d0;
+}
+
+__device__ __forceinline__ void atomic_add_i64(int64_t* p, int64_t v)
+{
+    atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
+}
+
+// Block-wide exclusive scan of one int per thread; returns the thread's prefix
+// and writes the block total to *total (all threads).
+template <int NT>
+__device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp, int* total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = (lane < NT / 32) ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < NT / 32) s_warp[lane] = w;
+    }
+    __syncthreads();
+    int prefix = (wid ? s_warp[wid - 1] : 0) + x - v;
+    *total = s_warp[NT / 32 - 1];
+    __syncthreads();
+    return prefix;
+}
+
+// Shared memory used by the load-balanced frontier walker.
+template <int NT>
+struct LbSmem {
+    int x[NT];
+    int off[NT];
+    int64_t row[NT];
+    int warp[NT / 32];
+};
+
+// Edge-balanced walk over the neighbours of a vertex list given as up to two
+// ranges (l1[0..n1) then l2[0..n2)).  Vertices are taken NT at a time; each
+// thread runs prep(j, x, visible_degree) for its vertex, an exclusive scan of
+// the visible degrees spreads the chunk's edges evenly over the block, and
+// edge(j, x, k) runs once per visible neighbour k (consecutive threads read
+// consecutive adjacency slots).  post(j, x) runs after the chunk's edges.
+// Ends with a block barrier.
+template <int NT, class Prep, class Edge, class Post>
+__device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t* l1, int n1,
+                                        const int32_t* l2, int n2, LbSmem<NT>& sm, Prep prep,
+                                        Edge edge, Post post)
+{
+    const int n = n1 + n2;
+    for (int base = 0; base < n; base += NT) {
+        const int j = threadIdx.x;
+        const int cnt = min(NT, n - base);
+        int d = 0;
+        if (j < cnt) {
+            int idx = base + j;
+            int x = idx < n1 ? l1[idx] : l2[idx - n1];
+            int64_t rs = G.row[x];
+            d = vis_deg(G, x, rs, g);
+            sm.x[j] = x;
+            sm.row[j] = rs;
+            prep(j, x, d);
+        }
+        int total;
+        int off = block_exclusive_scan<NT>(d, sm.warp, &total);
+        if (j < cnt) sm.off[j] = off;
+        __syncthreads();
+        for (int e = threadIdx.x; e < total; e += NT) {
+            int lo = 0, hi = cnt - 1;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (sm.off[mid] <= e) lo = mid;
+                else hi = mid - 1;
+            }
+            int k = G.col[sm.row[lo] + (e - sm.off[lo])];
+            edge(lo, sm.x[lo], k);
+        }
+        __syncthreads();
+        if (j < cnt) post(j, sm.x[j]);
+        __syncthreads();
+    }
+}
+
+struct NoPost {
+    __device__ void operator()(int, int) const {}
+};
+
+}  // namespace sbc

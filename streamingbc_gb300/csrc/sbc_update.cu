@@ -1,0 +1,358 @@
+// Incremental BC update for edge insertions over K roots.
+//
+// Replaces insertEdgeStreamingBC's COARSE loop (src/streamingbc.c:88-226) and
+// the two insertion cases it dispatches to:
+//   |d| == 1  addEdgeWithoutMovementBrandes  (src/streamingbc_internal.c:11-248)
+//   |d|  > 1  moveUpTreeBrandes              (src/streamingbc_internal.c:251-603)
+// with the same parent-free method: parents/children are found by comparing
+// neighbour distances, and the case is picked by d(r,u) - d(r,v).
+//
+// Kernels:
+//   k_classify  one thread per root: a root stays in the batch's worklist iff
+//               some insertion of the batch joins two different levels at the
+//               batch start (otherwise no insertion of the batch can change
+//               the root's state, so it is culled for the whole batch).
+//   k_update    persistent CTAs; each takes a root from the worklist and applies
+//               every insertion of the batch to it in order.  One insertion on
+//               one root is a "job":
+//     descent  level-synchronous BFS from the deeper endpoint b.  |d|==1:
+//              children (dist = level+1) gain diffPath; |d|>1: neighbours with
+//              old dist >= new level+1 join the next level (moved if strictly
+//              deeper before) and gain diffPath.  A vertex is claimed for a
+//              level with a CAS on its step tag; diffPath sums are int64 atomics.
+//     re-level (|d|>1) every descent vertex gets new dist = new level of its step.
+//     ascent   new levels from deepest to 0.  Per level: phase A walks the
+//              descent vertices, phase B the ascent-only vertices claimed for
+//              this level (parents found at level+1, and, for |d|>1, same-level
+//              ex-parents of moved vertices found in phase A).  Each vertex's
+//              new delta is final when its level starts; it pushes
+//              newsigma[k]*(newdelta[x]+1)/newsigma[x] into each parent k, minus
+//              its old contribution when k is ascent-only (except the new edge),
+//              adds newdelta-olddelta to BC, and commits sigma/delta in place.
+//     reset    scratch of every touched vertex is cleared (O(touched)).
+// Results are exact for dist/sigma (integer atomics); BC/delta differ from the
+// reference only by floating-point summation order.
+#include <climits>
+#include "sbc_host.h"
+#include "sbc_internal.cuh"
+
+namespace sbc {
+
+struct UpdateArgs {
+    DevGraph G;
+    int64_t nv;
+    int nk;
+    const int64_t* roots;
+    int32_t* dist;
+    int64_t* sigma;
+    double* delta;
+    double* bc;
+    ScratchBase scr;
+    int nins;
+    const int32_t* ins_u;
+    const int32_t* ins_v;
+    const int32_t* ins_ok;
+    int all_visible;
+    const int* worklist;
+    const int* nwork;
+    int* work_counter;
+    unsigned long long* counters;  // vertices, edges, case1, case2
+};
+
+template <int NT>
+struct UpdSmem {
+    LbSmem<NT> lb;
+    int64_t dp[NT];
+    double wn[NT];
+    double wo[NT];
+    int fl[NT];
+    int item, qt, at, st;
+};
+
+template <int NT>
+__device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, const Scratch& W, int r,
+                                        int a, int b, bool moving, int g, unsigned long long& cv,
+                                        unsigned long long& ce)
+{
+    const int64_t nv = A.nv;
+    int32_t* D = A.dist + (size_t)r * nv;
+    int64_t* S = A.sigma + (size_t)r * nv;
+    double* Dl = A.delta + (size_t)r * nv;
+    const int root = (int)A.roots[r];
+    const int Lb = D[a] + 1;  // new level of b; equals D[b] when |d| == 1
+
+    if (threadIdx.x == 0) {
+        W.st[b] = 1;
+        W.dp[b] = S[a];
+        W.qd[0] = b;
+        W.lvl[0] = 0;
+        W.lvl[1] = 1;
+        sm.qt = 1;
+        sm.at = 0;
+        sm.st = 0;
+    }
+    __syncthreads();
+
+    // ---------------- descent ----------------
+    int step = 0, lo = 0, hi = 1;
+    while (lo < hi) {
+        const int L = Lb + step;
+        const int tag = step + 2;
+        lb_walk<NT>(
+            A.G, g, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
+            [&](int j, int x, int d) {
+                sm.dp[j] = W.dp[x];
+                cv++;
+                ce += (unsigned)d;
+            },
+            [&](int j, int x, int k) {
+                const int dk = D[k];
+                if (moving ? (dk <= L) : (dk != L + 1)) return;
+                int s = W.st[k];
+                if (s == 0) {
+                    int old = atomicCAS(&W.st[k], 0, tag);
+                    if (old == 0) {
+                        int p = atomicAdd(&sm.qt, 1);
+                        W.qd[p] = k;
+                        s = tag;
+                    } else {
+                        s = old;
+                    }
+                }
+                if ((s & SBC_STEP_MASK) != tag) return;
+                atomic_add_i64(&W.dp[k], sm.dp[j]);
+            },
+            NoPost());
+        lo = hi;
+        hi = sm.qt;
+        ++step;
+        if (threadIdx.x == 0) W.lvl[step + 1] = hi;
+    }
+    const int ndown = hi;
+    const int nsteps = step;
+
+    // ---------------- re-level (|d| > 1) ----------------
+    if (moving) {
+        for (int i = threadIdx.x; i < ndown; i += NT) {
+            const int k = W.qd[i];
+            const int s = W.st[k];
+            const int nl = Lb + (s & SBC_STEP_MASK) - 1;
+            if (D[k] != nl) {
+                D[k] = nl;
+                W.st[k] = s | SBC_MOVED;
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---------------- ascent ----------------
+    int L = 0;
+    auto prep = [&](int j, int x, int d) {
+        const int s = W.st[x];
+        const bool isDown = (s & SBC_STEP_MASK) != 0;
+        const bool mv = (s & SBC_MOVED) != 0;
+        const int64_t oS = S[x];
+        const double oD = Dl[x];
+        const double ac = W.acc[x];
+        const int64_t nS = isDown ? (mv ? W.dp[x] : oS + W.dp[x]) : oS;
+        const double nD = isDown ? ac : oD + ac;
+        sm.wn[j] = (nD + 1.0) / (double)nS;
+        sm.wo[j] = oS ? (oD + 1.0) / (double)oS : 0.0;
+        sm.fl[j] = (mv ? 1 : 0) | (x == b ? 2 : 0);
+        if (x != root) atomicAdd(&A.bc[x], nD - oD);
+        S[x] = nS;
+        Dl[x] = nD;
+        cv++;
+        ce += (unsigned)d;
+    };
+    auto parent_edge = [&](int j, int x, int k) -> bool {
+        const int dk = D[k];
+        if (dk != L - 1) return false;
+        const int sk = W.st[k];
+        const bool kDown = (sk & SBC_STEP_MASK) != 0;
+        if (!kDown && !(sk & SBC_ASC)) {
+            int old = atomicOr(&W.st[k], SBC_ASC);
+            if (!(old & SBC_ASC)) {
+                int p = atomicAdd(&sm.at, 1);
+                W.qa[p] = k;
+            }
+        }
+        const int64_t nSk = kDown ? ((sk & SBC_MOVED) ? W.dp[k] : S[k] + W.dp[k]) : S[k];
+        double c = (double)nSk * sm.wn[j];
+        if (!kDown && !(k == a && (sm.fl[j] & 2))) c -= (double)S[k] * sm.wo[j];
+        atomicAdd(&W.acc[k], c);
+        return true;
+    };
+
+    int ua_lo = 0, ua_hi = 0;
+    const int Lmax = Lb + nsteps - 1;
+    for (L = Lmax; L >= 0; --L) {
+        const int ds = L - Lb;
+        const int32_t* dlist = nullptr;
+        int dn = 0;
+        if (ds >= 0) {
+            dlist = W.qd + W.lvl[ds];
+            dn = W.lvl[ds + 1] - W.lvl[ds];
+        }
+        const int next_lo = sm.at;
+        if (!moving) {
+            lb_walk<NT>(A.G, g, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,
+                        [&](int j, int x, int k) { parent_edge(j, x, k); }, NoPost());
+        } else {
+            const int same_lo = sm.st;
+            lb_walk<NT>(
+                A.G, g, dlist, dn, nullptr, 0, sm.lb, prep,
+                [&](int j, int x, int k) {
+                    if (parent_edge(j, x, k)) return;
+                    if (!(sm.fl[j] & 1) || D[k] != L) return;
+                    // k kept its level and lost the moved vertex x as a child
+                    const int sk = W.st[k];
+                    if (sk & SBC_STEP_MASK) return;
+                    if (!(sk & SBC_ASC)) {
+                        int old = atomicOr(&W.st[k], SBC_ASC);
+                        if (!(old & SBC_ASC)) {
+                            int p = atomicAdd(&sm.st, 1);
+                            W.qs[p] = k;
+                        }
+                    }
+                    atomicAdd(&W.acc[k], -(double)S[k] * sm.wo[j]);
+                },
+                NoPost());
+            const int same_hi = sm.st;
+            lb_walk<NT>(A.G, g, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
+                        prep, [&](int j, int x, int k) { parent_edge(j, x, k); }, NoPost());
+        }
+        ua_lo = next_lo;
+        ua_hi = sm.at;
+        if (L <= Lb && ua_lo == ua_hi) break;
+    }
+
+    // ---------------- reset touched scratch ----------------
+    const int na = sm.at, ns = sm.st;
+    for (int i = threadIdx.x; i < ndown; i += NT) {
+        const int k = W.qd[i];
+        W.st[k] = 0;
+        W.dp[k] = 0;
+        W.acc[k] = 0.0;
+    }
+    for (int i = threadIdx.x; i < na; i += NT) {
+        const int k = W.qa[i];
+        W.st[k] = 0;
+        W.acc[k] = 0.0;
+    }
+    for (int i = threadIdx.x; i < ns; i += NT) {
+        const int k = W.qs[i];
+        W.st[k] = 0;
+        W.acc[k] = 0.0;
+    }
+    __syncthreads();
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_update(UpdateArgs A)
+{
+    __shared__ UpdSmem<NT> sm;
+    const int64_t nv = A.nv;
+    const Scratch W = A.scr.of(blockIdx.x, nv);
+    const int nwork = *A.nwork;
+    const int g_all = INT_MAX;
+    unsigned long long cv = 0, ce = 0, c1 = 0, c2 = 0;
+
+    for (;;) {
+        if (threadIdx.x == 0) sm.item = atomicAdd(A.work_counter, 1);
+        __syncthreads();
+        const int item = sm.item;
+        __syncthreads();
+        if (item >= nwork) break;
+        const int r = A.worklist[item];
+        const int32_t* D = A.dist + (size_t)r * nv;
+        for (int i = 0; i < A.nins; ++i) {
+            if (A.ins_ok[i] <= 0) continue;
+            const int u = A.ins_u[i], v = A.ins_v[i];
+            const int du = D[u], dv = D[v];
+            if (du == dv) continue;  // same level, or both unreachable
+            const int b = du > dv ? u : v;
+            const int a = du > dv ? v : u;
+            const int db = du > dv ? du : dv, da = du > dv ? dv : du;
+            const bool moving = (db == SBC_INF) || (db - da > 1);
+            if (threadIdx.x == 0) {
+                if (moving) c2++;
+                else c1++;
+            }
+            run_job<NT>(A, sm, W, r, a, b, moving, A.all_visible ? g_all : i, cv, ce);
+        }
+    }
+    atomicAdd(&A.counters[0], cv);
+    atomicAdd(&A.counters[1], ce);
+    if (threadIdx.x == 0) {
+        atomicAdd(&A.counters[2], c1);
+        atomicAdd(&A.counters[3], c2);
+    }
+}
+
+__global__ void k_classify(const int32_t* __restrict__ dist, int64_t nv, int nk, int nins,
+                           const int32_t* __restrict__ iu, const int32_t* __restrict__ iv,
+                           const int32_t* __restrict__ ok, int* __restrict__ worklist, int* __restrict__ nwork)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nk) return;
+    const int32_t* D = dist + (size_t)r * nv;
+    bool active = false;
+    for (int i = 0; i < nins && !active; ++i)
+        if (ok[i] > 0 && D[iu[i]] != D[iv[i]]) active = true;
+    if (active) {
+        int p = atomicAdd(nwork, 1);
+        worklist[p] = r;
+    }
+}
+
+constexpr int kUpdateThreads = 256;
+
+int update_workers_per_sm()
+{
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_update<kUpdateThreads>, kUpdateThreads, 0);
+    return n;
+}
+
+cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
+{
+    sbc_graph* g = f->g;
+    cudaStream_t s = g->stream;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(f->d_nwork, 0, 2 * sizeof(int), s))) return e;  // nwork, counter
+    const int32_t* iu = g->d_ins;
+    const int32_t* iv = g->d_ins + g->ins_capacity;
+    const int32_t* ok = g->d_ins + 2 * g->ins_capacity;
+    f->prof_begin(PROF_CLASSIFY);
+    k_classify<<<(int)((f->nk + 255) / 256), 256, 0, s>>>(f->d_dist, f->nv, (int)f->nk, n, iu, iv, ok,
+                                                          f->d_worklist, f->d_nwork);
+    f->prof_end(PROF_CLASSIFY);
+    if ((e = cudaGetLastError())) return e;
+    UpdateArgs A;
+    A.G = g->dev();
+    A.nv = f->nv;
+    A.nk = (int)f->nk;
+    A.roots = f->d_roots;
+    A.dist = f->d_dist;
+    A.sigma = f->d_sigma;
+    A.delta = f->d_delta;
+    A.bc = f->d_bc;
+    A.scr = f->scratch();
+    A.nins = n;
+    A.ins_u = iu;
+    A.ins_v = iv;
+    A.ins_ok = ok;
+    A.all_visible = all_visible ? 1 : 0;
+    A.worklist = f->d_worklist;
+    A.nwork = f->d_nwork;
+    A.work_counter = f->d_counter;
+    A.counters = f->d_counters;
+    const int grid = (int)std::min<int64_t>(f->workers, f->nk);
+    f->prof_begin(PROF_UPDATE);
+    k_update<kUpdateThreads><<<grid, kUpdateThreads, 0, s>>>(A);
+    f->prof_end(PROF_UPDATE);
+    return cudaGetLastError();
+}
+
+}  // namespace sbc

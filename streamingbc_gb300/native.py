@@ -1,0 +1,290 @@
+"""ctypes binding of libsbc_gb300.so (the C-ABI in include/sbc_gb300.h and the
+drop-in streamingbc.h / stinger.h surface).
+
+This is how the tests and the benchmark call the CUDA path: through the same
+exported C symbols a reference-side caller would bind.  Loading fails loudly
+when the library is missing; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "libsbc_gb300.so")
+INCLUDE = os.path.join(ROOT, "include")
+
+_i64p = C.POINTER(C.c_int64)
+_i32p = C.POINTER(C.c_int32)
+_f64p = C.POINTER(C.c_double)
+_vp = C.c_void_p
+
+
+class SbcError(RuntimeError):
+    pass
+
+
+class BatchStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("inserted", "duplicates", "invalid", "roots_active", "case1", "case2",
+                                          "vertices", "edges")]
+
+    def as_dict(self) -> dict:
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class Profile(C.Structure):
+    _fields_ = [("static_ms", C.c_double), ("static_launches", C.c_int64),
+                ("append_ms", C.c_double), ("append_launches", C.c_int64),
+                ("classify_ms", C.c_double), ("classify_launches", C.c_int64),
+                ("update_ms", C.c_double), ("update_launches", C.c_int64),
+                ("batch_ms", C.c_double), ("batches", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {n: (float(getattr(self, n)) if t is C.c_double else int(getattr(self, n))) for n, t in self._fields_}
+
+
+def header_functions() -> list[str]:
+    """Every function name declared in include/*.h."""
+    names = []
+    for h in sorted(os.listdir(INCLUDE)):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(INCLUDE, h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"([A-Za-z_][A-Za-z0-9_]*)\s*\(([^;{}]*)\)\s*;", text):
+            name = m.group(1)
+            if name in ("if", "while", "for", "sizeof", "return"):
+                continue
+            names.append(name)
+    return sorted(set(names))
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the library (no build, no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise SbcError(f"{path} is missing: build it with streamingbc_gb300.build.build()")
+    lib = C.CDLL(path)
+    sig = {
+        "sbc_last_error": (C.c_char_p, []),
+        "sbc_set_device": (C.c_int, [C.c_int]),
+        "sbc_graph_create": (C.c_int, [C.POINTER(_vp), C.c_int64, _i64p, _i64p]),
+        "sbc_graph_destroy": (C.c_int, [_vp]),
+        "sbc_graph_num_vertices": (C.c_int, [_vp, _i64p]),
+        "sbc_graph_degree": (C.c_int, [_vp, C.c_int64, _i64p]),
+        "sbc_graph_insert_directed": (C.c_int, [_vp, C.c_int64, C.c_int64, C.POINTER(C.c_int)]),
+        "sbc_graph_to_csr": (C.c_int, [_vp, _i64p, _i64p]),
+        "sbc_graph_reserve": (C.c_int, [_vp, C.c_int64, _i64p, _i64p]),
+        "sbc_graph_repacks": (C.c_int, [_vp, _i64p]),
+        "sbc_forest_create": (C.c_int, [C.POINTER(_vp), _vp, C.c_int64, _i64p, C.c_int64]),
+        "sbc_forest_destroy": (C.c_int, [_vp]),
+        "sbc_forest_info": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p]),
+        "sbc_static_init": (C.c_int, [_vp]),
+        "sbc_insert_batch": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
+        "sbc_insert_batch_device": (C.c_int, [_vp, C.c_int64, _vp, _vp]),
+        "sbc_update_inserted": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
+        "sbc_sync": (C.c_int, [_vp]),
+        "sbc_read_counters": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p]),
+        "sbc_get_bc": (C.c_int, [_vp, _f64p]),
+        "sbc_get_dist": (C.c_int, [_vp, C.c_int64, C.c_int64, _i32p]),
+        "sbc_get_sigma": (C.c_int, [_vp, C.c_int64, C.c_int64, _i64p]),
+        "sbc_get_delta": (C.c_int, [_vp, C.c_int64, C.c_int64, _f64p]),
+        "sbc_set_profiling": (C.c_int, [_vp, C.c_int]),
+        "sbc_get_profile": (C.c_int, [_vp, C.POINTER(Profile)]),
+        "sbc_reset_profile": (C.c_int, [_vp]),
+        "sbc_timer_start": (C.c_int, [_vp]),
+        "sbc_timer_stop": (C.c_int, [_vp, _f64p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        msg = _lib.sbc_last_error().decode() if _lib else ""
+        raise SbcError(f"sbc error {rc}: {msg}")
+
+
+def _a64(x) -> np.ndarray:
+    return np.ascontiguousarray(x, dtype=np.int64)
+
+
+def p64(a: np.ndarray):
+    return a.ctypes.data_as(_i64p)
+
+
+class DeviceGraph:
+    """sbc_graph: the device slack-CSR adjacency."""
+
+    def __init__(self, nv: int, off, adj):
+        self.lib = load()
+        self._off = _a64(off)
+        self._adj = _a64(adj)
+        h = _vp()
+        _check(self.lib.sbc_graph_create(C.byref(h), int(nv), p64(self._off), p64(self._adj)))
+        self.h = h
+        self.nv = int(nv)
+
+    def degree(self, v: int) -> int:
+        d = C.c_int64()
+        _check(self.lib.sbc_graph_degree(self.h, int(v), C.byref(d)))
+        return d.value
+
+    def insert_directed(self, a: int, b: int) -> int:
+        r = C.c_int()
+        _check(self.lib.sbc_graph_insert_directed(self.h, int(a), int(b), C.byref(r)))
+        return r.value
+
+    def reserve(self, pairs):
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        u = np.ascontiguousarray(pairs[:, 0])
+        v = np.ascontiguousarray(pairs[:, 1])
+        _check(self.lib.sbc_graph_reserve(self.h, u.size, p64(u), p64(v)))
+
+    def repacks(self) -> int:
+        c = C.c_int64()
+        _check(self.lib.sbc_graph_repacks(self.h, C.byref(c)))
+        return c.value
+
+    def to_csr(self):
+        off = np.zeros(self.nv + 1, dtype=np.int64)
+        _check(self.lib.sbc_graph_to_csr(self.h, p64(off), None))
+        adj = np.zeros(int(off[-1]), dtype=np.int64)
+        _check(self.lib.sbc_graph_to_csr(self.h, p64(off), p64(adj)))
+        return off, adj
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sbc_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceForest:
+    """sbc_forest: per-root dist/sigma/delta and BC on the device."""
+
+    def __init__(self, graph: DeviceGraph, roots, workers: int = 0):
+        self.lib = load()
+        self.graph = graph
+        self.roots = _a64(roots)
+        h = _vp()
+        _check(self.lib.sbc_forest_create(C.byref(h), graph.h, self.roots.size, p64(self.roots), int(workers)))
+        self.h = h
+        self.nv = graph.nv
+        self.nk = int(self.roots.size)
+
+    def info(self) -> dict:
+        v = [C.c_int64() for _ in range(4)]
+        _check(self.lib.sbc_forest_info(self.h, *[C.byref(x) for x in v]))
+        return {"nv": v[0].value, "nk": v[1].value, "workers": v[2].value, "bytes": v[3].value}
+
+    def static_init(self, sync: bool = True):
+        _check(self.lib.sbc_static_init(self.h))
+        if sync:
+            self.sync()
+
+    def insert(self, pairs) -> dict:
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        u = np.ascontiguousarray(pairs[:, 0])
+        v = np.ascontiguousarray(pairs[:, 1])
+        st = BatchStats()
+        _check(self.lib.sbc_insert_batch(self.h, u.size, p64(u), p64(v), C.byref(st)))
+        return st.as_dict()
+
+    def insert_device(self, n: int, d_u: int, d_v: int):
+        """Asynchronous batch from int32 device pointers (e.g. tensor.data_ptr())."""
+        _check(self.lib.sbc_insert_batch_device(self.h, int(n), _vp(d_u), _vp(d_v)))
+
+    def update_inserted(self, pairs) -> dict:
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        u = np.ascontiguousarray(pairs[:, 0])
+        v = np.ascontiguousarray(pairs[:, 1])
+        st = BatchStats()
+        _check(self.lib.sbc_update_inserted(self.h, u.size, p64(u), p64(v), C.byref(st)))
+        return st.as_dict()
+
+    def sync(self):
+        _check(self.lib.sbc_sync(self.h))
+
+    def counters(self) -> dict:
+        v = [C.c_int64() for _ in range(4)]
+        _check(self.lib.sbc_read_counters(self.h, *[C.byref(x) for x in v]))
+        return {"vertices": v[0].value, "edges": v[1].value, "case1": v[2].value, "case2": v[3].value}
+
+    def bc(self) -> np.ndarray:
+        out = np.zeros(self.nv, dtype=np.float64)
+        _check(self.lib.sbc_get_bc(self.h, out.ctypes.data_as(_f64p)))
+        return out
+
+    def dist(self, r0: int = 0, nr: int | None = None) -> np.ndarray:
+        nr = self.nk - r0 if nr is None else nr
+        out = np.zeros((nr, self.nv), dtype=np.int32)
+        _check(self.lib.sbc_get_dist(self.h, r0, nr, out.ctypes.data_as(_i32p)))
+        return out
+
+    def sigma(self, r0: int = 0, nr: int | None = None) -> np.ndarray:
+        nr = self.nk - r0 if nr is None else nr
+        out = np.zeros((nr, self.nv), dtype=np.int64)
+        _check(self.lib.sbc_get_sigma(self.h, r0, nr, p64(out)))
+        return out
+
+    def delta(self, r0: int = 0, nr: int | None = None) -> np.ndarray:
+        nr = self.nk - r0 if nr is None else nr
+        out = np.zeros((nr, self.nv), dtype=np.float64)
+        _check(self.lib.sbc_get_delta(self.h, r0, nr, out.ctypes.data_as(_f64p)))
+        return out
+
+    def level64(self, r0: int = 0, nr: int | None = None) -> np.ndarray:
+        """dist widened to the reference convention (INT64_MAX = unreachable)."""
+        d = self.dist(r0, nr).astype(np.int64)
+        d[d == np.iinfo(np.int32).max] = np.iinfo(np.int64).max
+        return d
+
+    def set_profiling(self, on: bool):
+        _check(self.lib.sbc_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self) -> dict:
+        p = Profile()
+        _check(self.lib.sbc_get_profile(self.h, C.byref(p)))
+        return p.as_dict()
+
+    def reset_profile(self):
+        _check(self.lib.sbc_reset_profile(self.h))
+
+    def timer_start(self):
+        _check(self.lib.sbc_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        _check(self.lib.sbc_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sbc_forest_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

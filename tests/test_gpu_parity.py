@@ -1,0 +1,224 @@
+"""GPU parity tests: the sm_103a kernels, called through the C-ABI, against the
+golden vectors of the unmodified reference and against the oracle.
+
+Bar: dist and sigma bit-exact (unreachable sets equal), BC within
+|a-b| <= 1e-9*max(|b|,1) in FP64, traversal counters equal to the reference's.
+"""
+import numpy as np
+import pytest
+
+from _util import (BC_RTOL, assert_bc, assert_levels, assert_sigma, bc_err, golden_cases, load_golden,
+                   widen_dist)
+from streamingbc_gb300 import graphs as G
+from streamingbc_gb300 import native
+
+pytestmark = pytest.mark.gpu
+
+
+def make(g_nv, off, adj, roots, workers=0):
+    dg = native.DeviceGraph(g_nv, off, adj)
+    f = native.DeviceForest(dg, roots, workers=workers)
+    return dg, f
+
+
+def check_state(f, lv, sg, bc, delta=None):
+    assert_levels(f.level64(), lv)
+    assert_sigma(f.sigma(), sg, lv)
+    assert_bc(f.bc(), bc)
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_static_matches_reference(sbc_lib, case):
+    z = load_golden(case)
+    dg, f = make(int(z["nv"]), z["off"], z["adj"], z["roots"])
+    f.static_init()
+    check_state(f, z["level0"], z["sigma0"], z["bc0"])
+    f.close()
+    dg.close()
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_each_insertion_matches_reference(sbc_lib, case):
+    """One insertion per call (the plain path), BC compared after every one,
+    counters compared with the reference's per-insertion counters."""
+    z = load_golden(case)
+    dg, f = make(int(z["nv"]), z["off"], z["adj"], z["roots"])
+    f.static_init()
+    f.counters()
+    for i, (u, v) in enumerate(z["ins"]):
+        st = f.insert([(u, v)])
+        assert st["inserted"] == 1
+        got = [st["vertices"], st["edges"], st["case1"], st["case2"]]
+        assert got == z["counters"][i].tolist(), f"counters after insertion {i}: {got} vs {z['counters'][i]}"
+        assert bc_err(f.bc(), z["bc_trace"][i]) <= BC_RTOL, f"bc after insertion {i}"
+    check_state(f, z["level1"], z["sigma1"], z["bc1"])
+    f.close()
+    dg.close()
+
+
+@pytest.mark.parametrize("case", golden_cases())
+@pytest.mark.parametrize("batch", [7, 64])
+def test_batched_insertions_match_reference(sbc_lib, case, batch):
+    """Insertions applied in batches (one persistent launch per batch, each root
+    applies the batch in order) end in the reference's state."""
+    z = load_golden(case)
+    dg, f = make(int(z["nv"]), z["off"], z["adj"], z["roots"])
+    f.static_init()
+    ins = z["ins"]
+    for s in range(0, len(ins), batch):
+        st = f.insert(ins[s:s + batch])
+        assert st["inserted"] == len(ins[s:s + batch])
+        last = min(s + batch, len(ins)) - 1
+        assert bc_err(f.bc(), z["bc_trace"][last]) <= BC_RTOL
+    check_state(f, z["level1"], z["sigma1"], z["bc1"])
+    f.close()
+    dg.close()
+
+
+@pytest.mark.parametrize("workers", [1, 3])
+def test_few_workers_same_result(sbc_lib, workers):
+    z = load_golden("rmat9")
+    dg, f = make(int(z["nv"]), z["off"], z["adj"], z["roots"], workers=workers)
+    f.static_init()
+    f.insert(z["ins"])
+    check_state(f, z["level1"], z["sigma1"], z["bc1"])
+
+
+def test_er1024_exact_every_insertion_vs_oracle(sbc_lib, port_lib):
+    """ER G(1024, 8192) seed 1, exact BC (K = 1024), 256 uniform insertions one
+    at a time; full state compared with the oracle after every insertion."""
+    g, roots, ins = G.workload("er1024")
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    check_state(f, o.level(), o.sigma(), o.bc())
+    for i, (u, v) in enumerate(ins):
+        o.insert(int(u), int(v))
+        st = f.insert([(u, v)])
+        c = o.counters()
+        assert (st["vertices"], st["edges"], st["case1"], st["case2"]) == \
+            (c["vertices"], c["edges"], c["case1"], c["case2"]), f"counters at {i}"
+        assert_levels(f.level64(), o.level())
+        assert_sigma(f.sigma(), o.sigma(), o.level())
+        assert_bc(f.bc(), o.bc(), f"bc after insertion {i}")
+    d_err = np.abs(f.delta() - o.delta()) / np.maximum(np.abs(o.delta()), 1.0)
+    assert d_err.max() <= BC_RTOL
+
+
+def test_chunglu_batches_vs_oracle(sbc_lib, port_lib):
+    """Chung-Lu n=40000 (~176k edges, LCC), K = 256, 512 insertions (70% at BFS
+    distance <= 3) in batches of 64, state checked after every batch."""
+    g, roots, ins = G.workload("chunglu40k")
+    ins = ins[:512]
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    check_state(f, o.level(), o.sigma(), o.bc())
+    for s in range(0, len(ins), 64):
+        for u, v in ins[s:s + 64]:
+            o.insert(int(u), int(v))
+        f.insert(ins[s:s + 64])
+        check_state(f, o.level(), o.sigma(), o.bc())
+
+
+def test_rmat_incremental_equals_static_recompute(sbc_lib):
+    """Size-independent property on R-MAT scale 16: the incremental state after
+    1024 R-MAT-drawn insertions (batches of 64) equals a static recompute on
+    the updated graph (dist/sigma bit-exact, BC within tolerance)."""
+    g = G.rmat(16, 16, seed=3)
+    roots = G.pick_roots(g.nv, 256, 3)
+    ins = G.rmat_insertions(g, 16, 1024, seed=3)
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    for s in range(0, len(ins), 64):
+        f.insert(ins[s:s + 64])
+    g2 = G.insert_edges(g, ins)
+    dg2, f2 = make(g2.nv, g2.off, g2.adj, roots)
+    f2.static_init()
+    for r0 in range(0, 256, 64):
+        d1, d2 = f.dist(r0, 64), f2.dist(r0, 64)
+        assert np.array_equal(d1, d2)
+        reach = d2 != np.iinfo(np.int32).max
+        assert np.array_equal(f.sigma(r0, 64)[reach], f2.sigma(r0, 64)[reach])
+    assert_bc(f.bc(), f2.bc())
+
+
+def test_rejects_duplicates_and_loops(sbc_lib):
+    z = load_golden("er200")
+    dg, f = make(int(z["nv"]), z["off"], z["adj"], z["roots"])
+    f.static_init()
+    before = f.bc()
+    u = int(z["adj"][0])
+    existing = (0, u) if z["off"][1] > 0 else None
+    pairs = [(5, 5), (0, 10**9)]
+    if existing:
+        pairs.append(existing)
+    st = f.insert(pairs)
+    assert st["inserted"] == 0 and st["invalid"] == 2 and st["duplicates"] == (1 if existing else 0)
+    assert np.array_equal(f.bc(), before)
+    # duplicate inside one batch: the second copy is rejected
+    new = tuple(int(x) for x in z["ins"][0])
+    st = f.insert([new, new[::-1]])
+    assert st["inserted"] == 1 and st["duplicates"] == 1
+    assert bc_err(f.bc(), z["bc_trace"][0]) <= BC_RTOL
+
+
+def test_slack_repack_keeps_results(sbc_lib, port_lib):
+    """Many insertions at one vertex overflow its slack and force a re-pack of
+    the adjacency; results stay equal to the oracle."""
+    g = G.er(400, 800, seed=12)
+    roots = G.pick_roots(g.nv, 400, 0)
+    hub = 7
+    others = [v for v in range(g.nv) if v != hub and v not in set(g.adj[g.off[hub]:g.off[hub + 1]].tolist())]
+    ins = np.array([(hub, v) for v in others[:60]], dtype=np.int64)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    for s in range(0, len(ins), 16):
+        for u, v in ins[s:s + 16]:
+            o.insert(int(u), int(v))
+        f.insert(ins[s:s + 16])
+    check_state(f, o.level(), o.sigma(), o.bc())
+    assert dg.repacks() >= 1
+    off, adj = dg.to_csr()
+    assert off[hub + 1] - off[hub] == (g.off[hub + 1] - g.off[hub]) + 60
+
+
+def test_edge_cases_isolated_root_and_tiny_graphs(sbc_lib, port_lib):
+    # graph with an isolated root, a path, and insertions touching the root
+    n = 12
+    g = G.from_edges(n, np.array([1, 2, 3, 4, 6, 7]), np.array([2, 3, 4, 5, 7, 8]))
+    roots = np.arange(n)
+    ins = np.array([(0, 1), (5, 6), (0, 9), (9, 10), (3, 8), (1, 5)], dtype=np.int64)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots, nthreads=1)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    check_state(f, o.level(), o.sigma(), o.bc())
+    for u, v in ins:
+        o.insert(int(u), int(v))
+        f.insert([(u, v)])
+        check_state(f, o.level(), o.sigma(), o.bc())
+    # single root, single vertex
+    g1 = G.from_edges(1, np.array([], dtype=np.int64), np.array([], dtype=np.int64))
+    dg1, f1 = make(1, g1.off, g1.adj, np.array([0]))
+    f1.static_init()
+    assert f1.dist().tolist() == [[0]] and f1.bc().tolist() == [0.0]
+
+
+def test_device_batch_entry_point(sbc_lib):
+    torch = pytest.importorskip("torch")
+    z = load_golden("rmat9")
+    dg, f = make(int(z["nv"]), z["off"], z["adj"], z["roots"])
+    f.static_init()
+    dg.reserve(z["ins"])
+    ins = torch.tensor(z["ins"], dtype=torch.int32, device="cuda")
+    u = ins[:, 0].contiguous()
+    v = ins[:, 1].contiguous()
+    torch.cuda.synchronize()
+    f.insert_device(u.numel(), u.data_ptr(), v.data_ptr())
+    f.sync()
+    check_state(f, z["level1"], z["sigma1"], z["bc1"])
