@@ -1,0 +1,388 @@
+"""Benchmark: BC edge-insertion updates/s at K roots (plus p50/p99 latency)
+on one GB300, against the plain one-insertion-at-a-time GPU path and the
+reference CPU path.
+
+Default workload (--workload rmat20): R-MAT scale 20 (1,048,576 vertices,
+edge factor 16, a/b/c/d = .57/.19/.19/.05), symmetrised and deduplicated,
+seed 3; K = 1024 uniformly sampled roots; insertions drawn by the same R-MAT
+process and filtered to new edges.  A step is one batch of B insertions
+applied to all K roots (append + classify/cull + persistent update + seal).
+
+Printed JSON line keys (rank 0): metric/value/unit (whole-job updates/s with
+insertions resident in HBM), e2e (same metric through the host C-ABI with
+host buffers: H2D of the batch and D2H of the BC vector every step), roofline
+of the dominant kernel (k_update, HBM-bound), cpu_baseline (the oracle port
+on a bounded sample, scaled to K roots), clocks sampled during the timed
+region, gpu_launches, plain_gpu (one insertion per call), latency_ms.
+
+--impl reference times the reference algorithm on the host instead (the
+oracle port, all host threads) and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BC edge-insertion updates/s at K roots"
+UNIT = "insertions/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=["rmat20", "chunglu40k", "er1024"], default="rmat20")
+    p.add_argument("--batch", type=int, default=64)
+    p.add_argument("--plain", type=int, default=16, help="insertions timed on the plain one-at-a-time path")
+    p.add_argument("--cpu-roots", type=int, default=0, help="roots in the CPU sample (0 = 2 x host threads)")
+    p.add_argument("--cpu-insertions", type=int, default=16)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def workload_desc(name, g, roots):
+    if name == "rmat20":
+        return (f"rmat20: R-MAT scale 20, edge factor 16, a/b/c/d .57/.19/.19/.05, seed 3, symmetrised+deduplicated "
+                f"({g.nv} vertices, {g.ne} edges); K={len(roots)} uniform roots; R-MAT-drawn new-edge insertions")
+    if name == "chunglu40k":
+        return (f"chunglu40k: Chung-Lu n=40000, gamma 2.5, degrees [1,300], seed 2, LCC ({g.nv} vertices, {g.ne} "
+                f"edges); K={len(roots)}; insertions 70% at BFS distance <= 3")
+    return f"er1024: ER G(1024, 8192) seed 1, exact K=1024; uniform non-edge insertions"
+
+
+def load_workload(name, count):
+    from streamingbc_gb300 import graphs as G
+    if name == "rmat20":
+        g = G.rmat(20, 16, seed=3)
+        return g, G.pick_roots(g.nv, 1024, 3), G.rmat_insertions(g, 20, count, seed=3)
+    if name == "chunglu40k":
+        g = G.chung_lu(40000, 176000, 2.5, 1.0, 300.0, seed=2)
+        return g, G.pick_roots(g.nv, 256, 2), G.local_insertions(g, max(count, 4096), seed=2)[:count]
+    g = G.er(1024, 8192, seed=1)
+    return g, G.pick_roots(g.nv, g.nv, 1), G.uniform_insertions(g, count, seed=1)
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def barrier_max(value: float, world: int) -> float:
+    """Max over ranks (replicas); a no-op on one process."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_sample(g, roots, ins, n_roots, n_ins, threads):
+    """Oracle port (the reference algorithm in C, OpenMP over roots) on a
+    bounded sample: n_roots of the K roots, the first n_ins insertions.
+    Per-insertion time at K roots = per-root part * K/n_roots + BC reduce."""
+    from oracle import oracle as orc
+    orc.build()
+    sample_roots = roots[:n_roots]
+    o = orc.PortOracle(g.nv, g.off, g.adj, sample_roots, nthreads=threads)
+    t_static = o.static_timed()
+    per = []
+    for u, v in ins[:n_ins]:
+        tr, tb = o.insert_timed(int(u), int(v))
+        per.append(tr * (len(roots) / n_roots) + tb)
+    o.close()
+    mean = float(np.mean(per))
+    return {"value": 1.0 / mean, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n_roots} of {len(roots)} roots, first {n_ins} insertions; per-insertion per-root time "
+                      f"scaled x{len(roots) / n_roots:g}, BC reduce (O(NV*threads)) added once",
+            "per_insertion_ms": {"mean": mean * 1e3, "p50": float(np.percentile(per, 50)) * 1e3,
+                                 "p99": float(np.percentile(per, 99)) * 1e3},
+            "static_sample_s": t_static}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    need = args.warmup + args.steps
+    g, roots, ins = load_workload(args.workload, need)
+    n_roots = args.cpu_roots or min(len(roots), 2 * threads)
+    from oracle import oracle as orc
+    orc.build()
+    o = orc.PortOracle(g.nv, g.off, g.adj, roots[:n_roots], nthreads=threads)
+    o.static_timed()
+    times = []
+    for i, (u, v) in enumerate(ins[:need]):
+        tr, tb = o.insert_timed(int(u), int(v))
+        if i >= args.warmup:
+            times.append(tr * (len(roots) / n_roots) + tb)
+    o.close()
+    total = float(np.sum(times))
+    value = len(times) / total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total / len(times) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": workload_desc(args.workload, g, roots), "roots": int(len(roots)),
+                       "step": "one insertion applied to all K roots (the reference applies insertions one at a time)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n_roots} of {len(roots)} roots per insertion; per-root time scaled "
+                                       f"x{len(roots) / n_roots:g}, BC reduce added once"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from streamingbc_gb300 import build as b
+    from streamingbc_gb300 import native
+    if not os.path.exists(native.LIB_PATH):
+        b.build()
+    lib = native.load()
+    lib.sbc_set_device(local if world > 1 else 0)
+
+    B = args.batch
+    n_dev = (args.warmup + args.steps) * B
+    n_e2e = 0 if args.no_e2e else (1 + args.steps) * B
+    n_plain = args.plain
+    t0 = time.time()
+    g, roots, ins = load_workload(args.workload, n_dev + n_e2e + n_plain)
+    gen_s = time.time() - t0
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    dg.reserve(ins)  # slack for every insertion of the run, planned before timing
+
+    t0 = time.time()
+    f.static_init()
+    static_s = time.time() - t0
+    f.counters()
+
+    # ---------------- device-resident batches (value) ----------------
+    d_ins = torch.tensor(ins[:n_dev], dtype=torch.int32, device="cuda")
+    d_u = d_ins[:, 0].contiguous()
+    d_v = d_ins[:, 1].contiguous()
+    torch.cuda.synchronize()
+    for s in range(args.warmup):
+        f.insert_device(B, d_u[s * B:].data_ptr(), d_v[s * B:].data_ptr())
+    f.sync()
+    f.counters()
+    f.reset_profile()
+    f.set_profiling(True)
+    clk = ClockSampler(local)
+    clk.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    step_ms = []
+    f.timer_start()
+    t_wall = time.perf_counter()
+    for s in range(args.warmup, args.warmup + args.steps):
+        f.insert_device(B, d_u[s * B:].data_ptr(), d_v[s * B:].data_ptr())
+    total_ms = f.timer_stop()
+    wall_ms = (time.perf_counter() - t_wall) * 1e3
+    barrier(world)
+    clocks = clk.stop()
+    f.set_profiling(False)
+    prof = f.profile()
+    cnt = f.counters()
+    total_ms = barrier_max(total_ms, world)
+    n_timed = args.steps * B
+    value = n_timed * world / (total_ms / 1e3)
+
+    # per-batch latency: profiled batch events give each step's device time
+    batch_ms = prof["batch_ms"] / max(prof["batches"], 1)
+
+    # algorithmic bytes (compulsory traffic) of the timed region
+    K = len(roots)
+    alg_bytes = 8 * cnt["edges"] + 40 * cnt["vertices"] + 16 * K * n_timed
+    upd_launches = max(prof["update_launches"], 1)
+    upd_ms = prof["update_ms"] / upd_launches
+    achieved = (alg_bytes / upd_launches) / (upd_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"k_update_{args.workload}_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as fh:
+                tj = json.load(fh)
+            if tj.get("batch") == B:
+                traffic = tj.get("bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # ---------------- plain path: one insertion per call ----------------
+    plain = None
+    if n_plain:
+        pl = ins[n_dev + n_e2e:n_dev + n_e2e + n_plain]
+        lat = []
+        for u, v in pl:
+            t1 = time.perf_counter()
+            f.insert([(u, v)])
+            lat.append((time.perf_counter() - t1) * 1e3)
+        plain = {"value": 1e3 / float(np.mean(lat)), "unit": UNIT, "insertions": len(lat),
+                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                 "note": "sbc_insert_batch with n=1 per call (append + update + stats, synchronous)"}
+
+    # ---------------- e2e through the host C-ABI ----------------
+    e2e = None
+    if n_e2e:
+        base = n_dev
+        bc = np.zeros(g.nv, dtype=np.float64)
+        ei = np.ascontiguousarray(ins[base:base + n_e2e])
+        f.insert(ei[:B])  # warm-up step of this path
+        f.bc()
+        barrier(world)
+        lat = []
+        t1 = time.perf_counter()
+        for s in range(1, 1 + args.steps):
+            ts = time.perf_counter()
+            f.insert(ei[s * B:(s + 1) * B])
+            bc = f.bc()
+            lat.append((time.perf_counter() - ts) * 1e3)
+        e2e_s = barrier_max(time.perf_counter() - t1, world)
+        e2e = {"value": args.steps * B * world / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": 2 * 4 * B,
+               "d2h_bytes_per_step": 8 * g.nv + 4 * B + 4 + 32,
+               "p50_step_ms": float(np.percentile(lat, 50)), "p99_step_ms": float(np.percentile(lat, 99))}
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        threads = os.cpu_count() or 1
+        nr = args.cpu_roots or min(len(roots), 2 * threads)
+        cpu = cpu_sample(g, roots, ins, nr, args.cpu_insertions, threads)
+
+    info = f.info()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64+f64", "data": "synthetic",
+            "config": {"workload": workload_desc(args.workload, g, roots), "roots": K, "batch": B,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": f"per-root state {info['bytes'] / 1e9:.1f} GB on device >> 129 MB L2; no flush",
+                       "workers": info["workers"], "static_init_s": static_s, "generate_s": gen_s},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "k_update", "alg_bytes_per_launch": alg_bytes / upd_launches,
+                         "avg_launch_ms": upd_ms},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clocks,
+            "gpu_launches": 4 * args.steps,
+            "plain_gpu": plain,
+            "latency_ms": {"batch_p50": batch_ms, "wall_ms_timed": wall_ms,
+                           "per_insertion_in_batch": batch_ms},
+            "work": {"traversed_vertices": cnt["vertices"], "traversed_edges": cnt["edges"],
+                     "case1_pairs": cnt["case1"], "case2_pairs": cnt["case2"], "insertions": n_timed},
+            "kernel_ms": {k: prof[k] for k in ("append_ms", "classify_ms", "update_ms", "batch_ms")},
+        }
+        print(json.dumps(line), flush=True)
+    f.close()
+    dg.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -39,7 +39,8 @@ typedef struct sbc_forest sbc_forest;
 
 /* Per-call statistics of an insertion batch (counters match the reference's
  * COUNT_TRAVERSALS counters, src/streamingbc_internal.c:107-110,203-206,
- * 365-368,537-540, summed over roots). */
+ * 365-368,537-540, summed over roots).  A call that asks for statistics
+ * restarts the counters read by sbc_read_counters. */
 typedef struct {
     int64_t inserted;     /* insertions applied */
     int64_t duplicates;   /* rejected: edge already present */

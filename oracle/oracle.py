@@ -62,6 +62,9 @@ def _port_lib():
         lib.orc_static.argtypes = [C.c_void_p, C.c_void_p]
         lib.orc_insert.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64]
         lib.orc_classify.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.POINTER(C.c_int8)]
+        lib.orc_insert_timed.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, _f64p, _f64p]
+        lib.orc_static_timed.restype = C.c_double
+        lib.orc_static_timed.argtypes = [C.c_void_p, C.c_void_p]
         _port = lib
     return _port
 
@@ -108,6 +111,20 @@ class PortOracle:
         self.lib.orc_graph_insert(self.g, int(u), int(v))
         self.lib.orc_graph_insert(self.g, int(v), int(u))
         self.lib.orc_insert(self.f, self.g, int(u), int(v))
+
+    def static_timed(self) -> float:
+        return self.lib.orc_static_timed(self.f, self.g)
+
+    def insert_timed(self, u: int, v: int) -> tuple[float, float]:
+        """Like insert(); returns (seconds in the per-root updates, seconds in
+        the BC reduce).  The graph insertion itself is not timed, as in
+        updateEdgeNEW (src/sbcMain_utils.c:568-571)."""
+        self.lib.orc_graph_insert(self.g, int(u), int(v))
+        self.lib.orc_graph_insert(self.g, int(v), int(u))
+        a = C.c_double()
+        b = C.c_double()
+        self.lib.orc_insert_timed(self.f, self.g, int(u), int(v), C.byref(a), C.byref(b))
+        return a.value, b.value
 
     def classify(self, u: int, v: int) -> np.ndarray:
         out = np.zeros(self.nk, dtype=np.int8)

@@ -551,6 +551,34 @@ void orc_insert(orc_forest *f, const orc_graph *g, int64_t u, int64_t v)
     reduce_bc(f);
 }
 
+/* orc_insert with its two phases timed (wall seconds): the per-root updates
+ * (scale with the number of roots) and the per-thread BC reduce (O(NV*NT),
+ * independent of the number of roots). */
+void orc_insert_timed(orc_forest *f, const orc_graph *g, int64_t u, int64_t v, double *t_roots, double *t_reduce)
+{
+    double t0 = omp_get_wtime();
+    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt)
+    for (int64_t r = 0; r < f->nk; r++)
+        insert_root(g, f, r, u, v, &f->scr[omp_get_thread_num()]);
+    double t1 = omp_get_wtime();
+    reduce_bc(f);
+    double t2 = omp_get_wtime();
+    *t_roots = t1 - t0;
+    *t_reduce = t2 - t1;
+}
+
+/* Static init timed (wall seconds). */
+double orc_static_timed(orc_forest *f, const orc_graph *g)
+{
+    double t0 = omp_get_wtime();
+    for (int64_t x = 0; x < f->nv; x++) f->bc[x] = 0.0;
+    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt)
+    for (int64_t r = 0; r < f->nk; r++)
+        static_root(g, f, r, &f->scr[omp_get_thread_num()]);
+    reduce_bc(f);
+    return omp_get_wtime() - t0;
+}
+
 /* Per-insertion classification of every root at the current state:
  * out[r] = 0 (same level / both unreachable), 1 (|d| == 1), 2 (|d| > 1). */
 void orc_classify(const orc_forest *f, int64_t u, int64_t v, int8_t *out)

@@ -460,10 +460,7 @@ int sbc_forest_create(sbc_forest** out, sbc_graph* g, int64_t nk, const int64_t*
     CK(cudaMemsetAsync(f->d_acc, 0, sizeof(double) * sc, g->stream));
     CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * 4, g->stream));
     CK(cudaMemcpyAsync(f->d_roots, roots, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, g->stream));
-    for (int k = 0; k < sbc::PROF_COUNT; ++k) {
-        CK(cudaEventCreate(&f->ev_a[k]));
-        CK(cudaEventCreate(&f->ev_b[k]));
-    }
+    CK(f->prof_init());
     CK(cudaEventCreate(&f->t0));
     CK(cudaEventCreate(&f->t1));
     CK(cudaStreamSynchronize(g->stream));
@@ -493,10 +490,7 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_qa);
     dev_free(f->d_qs);
     dev_free(f->d_lvl);
-    for (int k = 0; k < sbc::PROF_COUNT; ++k) {
-        if (f->ev_a[k]) cudaEventDestroy(f->ev_a[k]);
-        if (f->ev_b[k]) cudaEventDestroy(f->ev_b[k]);
-    }
+    f->prof_release();
     if (f->t0) cudaEventDestroy(f->t0);
     if (f->t1) cudaEventDestroy(f->t1);
     delete f;
@@ -536,6 +530,8 @@ int sbc_insert_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* 
     int rc = plan_capacity(g, n, u, v, false);
     if (rc) return rc;
     if ((rc = stage_host(g, n, u, v, false))) return rc;
+    // per-call statistics cover this call only
+    if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * 4, g->stream));
     f->prof_begin(sbc::PROF_BATCH);
     f->prof_begin(sbc::PROF_APPEND);
     CK(sbc::launch_append(g, (int)n, false));
@@ -582,6 +578,7 @@ int sbc_update_inserted(sbc_forest* f, int64_t n, const int64_t* u, const int64_
     }
     int rc = stage_host(g, n, u, v, true);
     if (rc) return rc;
+    if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * 4, g->stream));
     f->prof_begin(sbc::PROF_BATCH);
     CK(sbc::launch_update(f, (int)n, true));
     f->prof_end(sbc::PROF_BATCH);

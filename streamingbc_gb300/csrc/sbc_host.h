@@ -75,11 +75,15 @@ struct sbc_forest {
     int* d_counter = nullptr; // [1]
     unsigned long long* d_counters = nullptr;  // [4]: vertices, edges, case1, case2
     int64_t bytes = 0;
-    // profiling: CUDA events around each kernel kind
+    // profiling: a ring of CUDA event pairs per kernel kind; pairs are read
+    // back only when the ring wraps or the profile is queried, so recording
+    // never makes the host wait for the device.
+    static constexpr int kRing = 512;
     bool prof = false;
-    cudaEvent_t ev_a[sbc::PROF_COUNT] = {};
-    cudaEvent_t ev_b[sbc::PROF_COUNT] = {};
-    bool ev_pending[sbc::PROF_COUNT] = {};
+    std::vector<cudaEvent_t> ev_a[sbc::PROF_COUNT];
+    std::vector<cudaEvent_t> ev_b[sbc::PROF_COUNT];
+    std::vector<char> ev_pending[sbc::PROF_COUNT];
+    int ev_next[sbc::PROF_COUNT] = {};
     double prof_ms[sbc::PROF_COUNT] = {};
     int64_t prof_n[sbc::PROF_COUNT] = {};
     cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -96,28 +100,58 @@ struct sbc_forest {
         s.lvl = d_lvl;
         return s;
     }
+    cudaError_t prof_init()
+    {
+        for (int k = 0; k < sbc::PROF_COUNT; ++k) {
+            ev_a[k].assign(kRing, nullptr);
+            ev_b[k].assign(kRing, nullptr);
+            ev_pending[k].assign(kRing, 0);
+            for (int i = 0; i < kRing; ++i) {
+                cudaError_t e;
+                if ((e = cudaEventCreate(&ev_a[k][i])) || (e = cudaEventCreate(&ev_b[k][i]))) return e;
+            }
+        }
+        return cudaSuccess;
+    }
+    void prof_release()
+    {
+        for (int k = 0; k < sbc::PROF_COUNT; ++k) {
+            for (auto e : ev_a[k])
+                if (e) cudaEventDestroy(e);
+            for (auto e : ev_b[k])
+                if (e) cudaEventDestroy(e);
+            ev_a[k].clear();
+            ev_b[k].clear();
+        }
+    }
+    void prof_collect_slot(int k, int i)
+    {
+        if (!ev_pending[k][i]) return;
+        float ms = 0.f;
+        cudaEventSynchronize(ev_b[k][i]);
+        cudaEventElapsedTime(&ms, ev_a[k][i], ev_b[k][i]);
+        prof_ms[k] += ms;
+        prof_n[k] += 1;
+        ev_pending[k][i] = 0;
+    }
     void prof_collect(int k)
     {
-        if (ev_pending[k]) {
-            float ms = 0.f;
-            cudaEventSynchronize(ev_b[k]);
-            cudaEventElapsedTime(&ms, ev_a[k], ev_b[k]);
-            prof_ms[k] += ms;
-            prof_n[k] += 1;
-            ev_pending[k] = false;
-        }
+        for (int i = 0; i < (int)ev_pending[k].size(); ++i) prof_collect_slot(k, i);
     }
     void prof_begin(int k)
     {
         if (!prof) return;
-        prof_collect(k);
-        cudaEventRecord(ev_a[k], g->stream);
+        const int i = ev_next[k];
+        prof_collect_slot(k, i);
+        cudaEventRecord(ev_a[k][i], g->stream);
     }
     void prof_end(int k)
     {
         if (!prof) return;
-        cudaEventRecord(ev_b[k], g->stream);
-        ev_pending[k] = true;
+        const int i = ev_next[k];
+        cudaEventRecord(ev_b[k][i], g->stream);
+        ev_pending[k][i] = 1;
+        ev_next[k] = (i + 1) % kRing;
     }
 };
 

@@ -55,21 +55,38 @@ def from_edges(nv: int, u: np.ndarray, v: np.ndarray) -> Graph:
     u, v = u[keep], v[keep]
     lo = np.minimum(u, v)
     hi = np.maximum(u, v)
-    key = np.unique(lo * nv + hi)
+    key = _sorted_unique(lo * nv + hi)
     lo, hi = key // nv, key % nv
-    src = np.concatenate([lo, hi])
-    dst = np.concatenate([hi, lo])
-    order = np.lexsort((dst, src))
-    src, dst = src[order], dst[order]
+    both = np.concatenate([key, hi * nv + lo])  # (u,v) and (v,u) as src*nv+dst
+    both.sort()
+    src = both // nv
+    dst = both - src * nv
     off = np.zeros(nv + 1, dtype=np.int64)
-    np.add.at(off, src + 1, 1)
-    np.cumsum(off, out=off)
+    off[1:] = np.cumsum(np.bincount(src, minlength=nv))
     return Graph(nv, off, dst.astype(np.int64))
 
 
+def _sorted_unique(keys: np.ndarray) -> np.ndarray:
+    """Sorted distinct values (sort + neighbour compare)."""
+    k = np.sort(keys)
+    if k.size == 0:
+        return k
+    m = np.empty(k.size, dtype=bool)
+    m[0] = True
+    np.not_equal(k[1:], k[:-1], out=m[1:])
+    return k[m]
+
+
 def _unique_in_order(keys: np.ndarray) -> np.ndarray:
-    _, first = np.unique(keys, return_index=True)
-    return keys[np.sort(first)]
+    """Distinct values in order of first appearance."""
+    order = np.argsort(keys, kind="stable")
+    k = keys[order]
+    if k.size == 0:
+        return k
+    m = np.empty(k.size, dtype=bool)
+    m[0] = True
+    np.not_equal(k[1:], k[:-1], out=m[1:])
+    return keys[np.sort(order[m])]
 
 
 def er(n: int, m: int, seed: int) -> Graph:
@@ -105,17 +122,37 @@ def largest_component(g: Graph) -> tuple[Graph, np.ndarray]:
     return from_edges(keep.size, remap[src[sel]], remap[g.adj[sel]]), keep
 
 
+def chung_lu_weights(n: int, m: int, gamma: float, dmin: float, dmax: float) -> np.ndarray:
+    """Expected degrees w_i = dmax * (1 + i/i0)^(-1/(gamma-1)), clipped below at
+    dmin, with i0 chosen so that sum(w) = 2m: a power-law degree tail of
+    exponent gamma, maximum expected degree dmax and m expected edges."""
+    i = np.arange(n, dtype=np.float64)
+    e = -1.0 / (gamma - 1.0)
+
+    def total(i0):
+        return np.maximum(dmin, dmax * (1.0 + i / i0) ** e).sum()
+
+    lo, hi = 1e-6, float(n) * 1e3
+    if total(hi) <= 2 * m:
+        i0 = hi
+    else:
+        for _ in range(200):
+            mid = np.sqrt(lo * hi)
+            if total(mid) < 2 * m:
+                lo = mid
+            else:
+                hi = mid
+        i0 = hi
+    return np.maximum(dmin, dmax * (1.0 + i / i0) ** e)
+
+
 def chung_lu(n: int, m: int, gamma: float, dmin: float, dmax: float, seed: int,
              lcc: bool = True) -> Graph:
-    """Chung-Lu graph: expected degree of vertex i follows a power law
-    w_i ~ (i + i0)^(-1/(gamma-1)) scaled into [dmin, dmax]; m distinct edges are
-    drawn with both endpoints sampled proportionally to w.  With ``lcc`` the
-    largest connected component is kept."""
+    """Chung-Lu graph with expected degrees from ``chung_lu_weights``: m
+    distinct edges are drawn with both endpoints sampled proportionally to w.
+    With ``lcc`` the largest connected component is kept."""
     rng = np.random.default_rng(seed)
-    i = np.arange(n, dtype=np.float64)
-    w = (i + 1.0) ** (-1.0 / (gamma - 1.0))
-    w = dmax * w / w[0]
-    w = np.maximum(w, dmin)
+    w = chung_lu_weights(n, m, gamma, dmin, dmax)
     p = w / w.sum()
     cdf = np.cumsum(p)
     got = np.empty(0, dtype=np.int64)
@@ -144,8 +181,10 @@ def _rmat_pairs(scale: int, count: int, a: float, b: float, c: float,
         r = rng.random(count)
         bu = r >= ab                      # quadrants c, d set the row bit
         bv = ((r >= a) & (r < ab)) | (r >= abc)  # quadrants b, d set the column bit
-        u = (u << 1) | bu
-        v = (v << 1) | bv
+        u <<= 1
+        v <<= 1
+        u |= bu
+        v |= bv
     return u, v
 
 
@@ -191,15 +230,19 @@ def _filter_new(g: Graph, u: np.ndarray, v: np.ndarray, taken: set[int]) -> list
     return out
 
 
+# Candidate pairs are drawn in chunks of this fixed size, so that a stream of
+# `count` insertions is a prefix of the stream for any larger count.
+_CHUNK = 4096
+
+
 def uniform_insertions(g: Graph, count: int, seed: int) -> np.ndarray:
     """``count`` distinct uniformly random vertex pairs that are not edges."""
     rng = np.random.default_rng(seed)
     taken: set[int] = set()
     out: list[tuple[int, int]] = []
     while len(out) < count:
-        need = count - len(out)
-        u = rng.integers(0, g.nv, size=2 * need + 16, dtype=np.int64)
-        v = rng.integers(0, g.nv, size=2 * need + 16, dtype=np.int64)
+        u = rng.integers(0, g.nv, size=_CHUNK, dtype=np.int64)
+        v = rng.integers(0, g.nv, size=_CHUNK, dtype=np.int64)
         out += _filter_new(g, u, v, taken)
     return np.asarray(out[:count], dtype=np.int64).reshape(-1, 2)
 
@@ -253,8 +296,7 @@ def rmat_insertions(g: Graph, scale: int, count: int, seed: int, a: float = 0.57
     taken: set[int] = set()
     out: list[tuple[int, int]] = []
     while len(out) < count:
-        need = count - len(out)
-        u, v = _rmat_pairs(scale, 2 * need + 64, a, b, c, rng)
+        u, v = _rmat_pairs(scale, _CHUNK, a, b, c, rng)
         out += _filter_new(g, u, v, taken)
     return np.asarray(out[:count], dtype=np.int64).reshape(-1, 2)
 
