@@ -44,13 +44,15 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["rmat20", "chunglu40k", "er1024"], default="rmat20")
+    p.add_argument("--workload", choices=["rmat20", "rmat18", "rmat16", "chunglu40k", "er1024"], default="rmat20")
     p.add_argument("--batch", type=int, default=64)
     p.add_argument("--plain", type=int, default=16, help="insertions timed on the plain one-at-a-time path")
     p.add_argument("--cpu-roots", type=int, default=0, help="roots in the CPU sample (0 = 2 x host threads)")
     p.add_argument("--cpu-insertions", type=int, default=16)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--variant", type=int, default=-1, help="update-kernel launch shape (-1 = library default)")
+    p.add_argument("--workers", type=int, default=0, help="persistent workers (0 = automatic)")
     return p.parse_args()
 
 
@@ -58,6 +60,9 @@ def workload_desc(name, g, roots):
     if name == "rmat20":
         return (f"rmat20: R-MAT scale 20, edge factor 16, a/b/c/d .57/.19/.19/.05, seed 3, symmetrised+deduplicated "
                 f"({g.nv} vertices, {g.ne} edges); K={len(roots)} uniform roots; R-MAT-drawn new-edge insertions")
+    if name in ("rmat16", "rmat18"):
+        return (f"{name}: R-MAT scale {name[4:]}, edge factor 16, seed 3 ({g.nv} vertices, {g.ne} edges); "
+                f"K={len(roots)} uniform roots; R-MAT-drawn new-edge insertions")
     if name == "chunglu40k":
         return (f"chunglu40k: Chung-Lu n=40000, gamma 2.5, degrees [1,300], seed 2, LCC ({g.nv} vertices, {g.ne} "
                 f"edges); K={len(roots)}; insertions 70% at BFS distance <= 3")
@@ -69,6 +74,12 @@ def load_workload(name, count):
     if name == "rmat20":
         g = G.rmat(20, 16, seed=3)
         return g, G.pick_roots(g.nv, 1024, 3), G.rmat_insertions(g, 20, count, seed=3)
+    if name == "rmat16":
+        g = G.rmat(16, 16, seed=3)
+        return g, G.pick_roots(g.nv, 256, 3), G.rmat_insertions(g, 16, count, seed=3)
+    if name == "rmat18":
+        g = G.rmat(18, 16, seed=3)
+        return g, G.pick_roots(g.nv, 512, 3), G.rmat_insertions(g, 18, count, seed=3)
     if name == "chunglu40k":
         g = G.chung_lu(40000, 176000, 2.5, 1.0, 300.0, seed=2)
         return g, G.pick_roots(g.nv, 256, 2), G.local_insertions(g, max(count, 4096), seed=2)[:count]
@@ -242,7 +253,7 @@ def run_ours(args):
     g, roots, ins = load_workload(args.workload, n_dev + n_e2e + n_plain)
     gen_s = time.time() - t0
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
-    f = native.DeviceForest(dg, roots)
+    f = native.DeviceForest(dg, roots, workers=args.workers, variant=args.variant)
     dg.reserve(ins)  # slack for every insertion of the run, planned before timing
 
     t0 = time.time()
@@ -352,7 +363,8 @@ def run_ours(args):
             "config": {"workload": workload_desc(args.workload, g, roots), "roots": K, "batch": B,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": f"per-root state {info['bytes'] / 1e9:.1f} GB on device >> 129 MB L2; no flush",
-                       "workers": info["workers"], "static_init_s": static_s, "generate_s": gen_s},
+                       "workers": info["workers"], "variant": args.variant, "static_init_s": static_s,
+                       "generate_s": gen_s},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_update", "alg_bytes_per_launch": alg_bytes / upd_launches,

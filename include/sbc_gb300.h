@@ -101,6 +101,14 @@ int sbc_graph_to_csr(sbc_graph *g, int64_t *off, int64_t *adj);
  * createExtraArraysForThreads (src/streamingbc_aux.c:234-296).  `workers`
  * persistent CTAs are sized from occupancy and free memory (0 = automatic). */
 int sbc_forest_create(sbc_forest **out, sbc_graph *g, int64_t nk, const int64_t *roots, int64_t workers);
+/* As sbc_forest_create with an explicit launch shape of the update kernel
+ * (variant -1: the SBC_UPDATE_VARIANT environment variable, else the default). */
+int sbc_forest_create_ex(sbc_forest **out, sbc_graph *g, int64_t nk, const int64_t *roots, int64_t workers,
+                         int variant);
+/* Launch shapes of the update kernel in this build: threads per CTA and the
+ * CTAs one SM keeps resident (results never depend on the shape). */
+int sbc_update_variant_count(int *count);
+int sbc_update_variant_info(int v, int *threads_per_cta, int *min_ctas_per_sm, int *ctas_per_sm);
 int sbc_forest_destroy(sbc_forest *f);
 /* nv, nk, workers, device bytes held by the forest. */
 int sbc_forest_info(const sbc_forest *f, int64_t *nv, int64_t *nk, int64_t *workers, int64_t *bytes);

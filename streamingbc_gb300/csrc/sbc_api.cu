@@ -400,10 +400,38 @@ int sbc_graph_to_csr(sbc_graph* g, int64_t* off, int64_t* adj)
 
 // ------------------------------------------------------------------ forest
 
+int sbc_update_variant_count(int* count)
+{
+    if (!count) return fail(SBC_ERR_ARG, "sbc_update_variant_count: null");
+    *count = sbc::update_variant_count();
+    return SBC_OK;
+}
+
+int sbc_update_variant_info(int v, int* threads_per_cta, int* min_ctas_per_sm, int* ctas_per_sm)
+{
+    if (v < 0 || v >= sbc::update_variant_count()) return fail(SBC_ERR_ARG, "update variant %d out of range", v);
+    if (threads_per_cta) *threads_per_cta = sbc::update_variant_threads(v);
+    if (min_ctas_per_sm) *min_ctas_per_sm = 0;
+    if (ctas_per_sm) *ctas_per_sm = sbc::update_workers_per_sm(v);
+    return SBC_OK;
+}
+
 int sbc_forest_create(sbc_forest** out, sbc_graph* g, int64_t nk, const int64_t* roots, int64_t workers)
+{
+    return sbc_forest_create_ex(out, g, nk, roots, workers, -1);
+}
+
+int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64_t* roots, int64_t workers,
+                         int variant)
 {
     if (!out || !g || nk <= 0 || !roots) return fail(SBC_ERR_ARG, "sbc_forest_create: bad arguments");
     *out = nullptr;
+    if (variant < 0) {
+        const char* env = getenv("SBC_UPDATE_VARIANT");
+        variant = env ? atoi(env) : sbc::update_default_variant();
+    }
+    if (variant < 0 || variant >= sbc::update_variant_count())
+        return fail(SBC_ERR_ARG, "update variant %d out of range", variant);
     if (nk > g->nv) return fail(SBC_ERR_ARG, "more roots (%lld) than vertices (%lld)", (long long)nk, (long long)g->nv);
     if (nk >= INT32_MAX) return fail(SBC_ERR_ARG, "too many roots");
     {
@@ -419,6 +447,7 @@ int sbc_forest_create(sbc_forest** out, sbc_graph* g, int64_t nk, const int64_t*
     f->g = g;
     f->nv = g->nv;
     f->nk = nk;
+    f->variant = variant;
     f->h_roots.assign(roots, roots + nk);
     cudaDeviceProp prop;
     CK(cudaGetDeviceProperties(&prop, g->device));
@@ -434,9 +463,10 @@ int sbc_forest_create(sbc_forest** out, sbc_graph* g, int64_t nk, const int64_t*
     f->d_counter = f->d_nwork + 1;
     f->bytes = (int64_t)(cells * 20 + f->nv * 8);
 
-    // Persistent workers: occupancy-limited, and their scratch (36 B per vertex
-    // each) limited to half of the memory still free.
-    int per_sm = std::min(sbc::update_workers_per_sm(), sbc::static_workers_per_sm());
+    // Persistent workers: as many as the update kernel keeps resident, and
+    // their scratch (36 B per vertex each) limited to half of the memory still
+    // free.  The static kernel runs over the same worker slots.
+    int per_sm = sbc::update_workers_per_sm(variant);
     if (per_sm < 1) per_sm = 1;
     int64_t w = workers > 0 ? workers : (int64_t)per_sm * f->sm_count;
     const size_t per_worker = (size_t)f->nv * 36 + 16;

@@ -62,6 +62,7 @@ struct sbc_forest {
     bool initialized = false;
     // persistent workers and their scratch
     int sm_count = 0;
+    int variant = 0;  // launch shape of the update kernel
     int64_t workers = 0;
     int32_t* d_st = nullptr;
     int64_t* d_dp = nullptr;
@@ -157,7 +158,10 @@ struct sbc_forest {
 
 namespace sbc {
 int static_workers_per_sm();
-int update_workers_per_sm();
+int update_variant_count();
+int update_default_variant();
+int update_variant_threads(int v);
+int update_workers_per_sm(int v);
 cudaError_t launch_static(sbc_forest* f);
 // Classify + cull + update for insertions already staged in g->d_ins
 // (u, v, ok rows).  `all_visible` ignores the per-slot sequence numbers.

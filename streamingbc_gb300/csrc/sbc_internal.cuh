@@ -119,53 +119,84 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp, int* tot
 template <int NT>
 struct LbSmem {
     int x[NT];
-    int off[NT];
+    int off[NT + 1];
     int64_t row[NT];
     int warp[NT / 32];
+    // traversal counters of the block: vertices walked and their visible degrees
+    unsigned long long walked_v, walked_e;
 };
+
+// Edges each thread has in flight per round of the walker: the adjacency
+// slots of all of them are loaded first, then all neighbour-distance gathers,
+// and only then are they processed, so a thread keeps kEdgeIlp independent
+// HBM reads outstanding instead of one.
+constexpr int kEdgeIlp = 4;
 
 // Edge-balanced walk over the neighbours of a vertex list given as up to two
 // ranges (l1[0..n1) then l2[0..n2)).  Vertices are taken NT at a time; each
 // thread runs prep(j, x, visible_degree) for its vertex, an exclusive scan of
 // the visible degrees spreads the chunk's edges evenly over the block, and
-// edge(j, x, k) runs once per visible neighbour k (consecutive threads read
-// consecutive adjacency slots).  post(j, x) runs after the chunk's edges.
-// Ends with a block barrier.
+// edge(j, x, k, D[k]) runs once per visible neighbour k (consecutive threads
+// read consecutive adjacency slots; D is the root's distance row, gathered by
+// the walker).  post(j, x) runs after the chunk's edges.  Ends with a barrier.
 template <int NT, class Prep, class Edge, class Post>
-__device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t* l1, int n1,
-                                        const int32_t* l2, int n2, LbSmem<NT>& sm, Prep prep,
-                                        Edge edge, Post post)
+__device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t* __restrict__ D,
+                                        const int32_t* l1, int n1, const int32_t* l2, int n2, LbSmem<NT>& sm,
+                                        Prep prep, Edge edge, Post post)
 {
     const int n = n1 + n2;
     for (int base = 0; base < n; base += NT) {
-        const int j = threadIdx.x;
+        const int t = threadIdx.x;
         const int cnt = min(NT, n - base);
         int d = 0;
-        if (j < cnt) {
-            int idx = base + j;
+        if (t < cnt) {
+            int idx = base + t;
             int x = idx < n1 ? l1[idx] : l2[idx - n1];
             int64_t rs = G.row[x];
             d = vis_deg(G, x, rs, g);
-            sm.x[j] = x;
-            sm.row[j] = rs;
-            prep(j, x, d);
+            sm.x[t] = x;
+            sm.row[t] = rs;
+            prep(t, x, d);
         }
         int total;
         int off = block_exclusive_scan<NT>(d, sm.warp, &total);
-        if (j < cnt) sm.off[j] = off;
-        __syncthreads();
-        for (int e = threadIdx.x; e < total; e += NT) {
-            int lo = 0, hi = cnt - 1;
-            while (lo < hi) {
-                int mid = (lo + hi + 1) >> 1;
-                if (sm.off[mid] <= e) lo = mid;
-                else hi = mid - 1;
-            }
-            int k = G.col[sm.row[lo] + (e - sm.off[lo])];
-            edge(lo, sm.x[lo], k);
+        if (t < cnt) sm.off[t] = off;
+        if (t == 0) {
+            sm.off[cnt] = total;
+            sm.walked_v += (unsigned)cnt;
+            sm.walked_e += (unsigned)total;
         }
         __syncthreads();
-        if (j < cnt) post(j, sm.x[j]);
+        int j = 0;  // chunk vertex of this thread's current edge; edges only move forward
+        for (int e0 = t; e0 < total; e0 += NT * kEdgeIlp) {
+            int kk[kEdgeIlp], jj[kEdgeIlp], dk[kEdgeIlp];
+#pragma unroll
+            for (int u = 0; u < kEdgeIlp; ++u) {
+                const int e = e0 + u * NT;
+                kk[u] = -1;
+                jj[u] = j;
+                if (e < total) {
+                    if (sm.off[j + 1] <= e) {
+                        int lo = j + 1, hi = cnt - 1;
+                        while (lo < hi) {
+                            int mid = (lo + hi + 1) >> 1;
+                            if (sm.off[mid] <= e) lo = mid;
+                            else hi = mid - 1;
+                        }
+                        j = lo;
+                    }
+                    jj[u] = j;
+                    kk[u] = G.col[sm.row[j] + (e - sm.off[j])];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kEdgeIlp; ++u) dk[u] = kk[u] >= 0 ? D[kk[u]] : 0;
+#pragma unroll
+            for (int u = 0; u < kEdgeIlp; ++u)
+                if (kk[u] >= 0) edge(jj[u], sm.x[jj[u]], kk[u], dk[u]);
+        }
+        __syncthreads();
+        if (t < cnt) post(t, sm.x[t]);
         __syncthreads();
     }
 }

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
     __shared__ double s_acc[NT];
     const int64_t nv = A.nv;
     Scratch W = A.scr.of(blockIdx.x, nv);
-    unsigned long long cv = 0, ce = 0;
+    if (threadIdx.x == 0) sm.walked_v = sm.walked_e = 0;
 
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(A.work_counter, 1);
@@ -73,14 +73,9 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         int L = 0, lo = 0, hi = 1;
         while (lo < hi) {
             lb_walk<NT>(
-                A.G, INT_MAX, W.qd + lo, hi - lo, nullptr, 0, sm,
-                [&](int j, int x, int d) {
-                    s_sig[j] = Sg[x];
-                    cv++;
-                    ce += (unsigned)d;
-                },
-                [&](int j, int x, int k) {
-                    int dk = D[k];
+                A.G, INT_MAX, D, W.qd + lo, hi - lo, nullptr, 0, sm,
+                [&](int j, int x, int d) { s_sig[j] = Sg[x]; },
+                [&](int j, int x, int k, int dk) {
                     if (dk == SBC_INF) {
                         int old = atomicCAS(&D[k], SBC_INF, L + 1);
                         if (old == SBC_INF) {
@@ -106,14 +101,10 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         for (int l = nlev - 1; l >= 0; --l) {
             const int b0 = W.lvl[l], b1 = W.lvl[l + 1];
             lb_walk<NT>(
-                A.G, INT_MAX, W.qd + b0, b1 - b0, nullptr, 0, sm,
-                [&](int j, int x, int d) {
-                    s_acc[j] = 0.0;
-                    cv++;
-                    ce += (unsigned)d;
-                },
-                [&](int j, int x, int k) {
-                    if (D[k] == l + 1) atomicAdd(&s_acc[j], W.acc[k]);
+                A.G, INT_MAX, D, W.qd + b0, b1 - b0, nullptr, 0, sm,
+                [&](int j, int x, int d) { s_acc[j] = 0.0; },
+                [&](int j, int x, int k, int dk) {
+                    if (dk == l + 1) atomicAdd(&s_acc[j], W.acc[k]);
                 },
                 [&](int j, int x) {
                     double sx = (double)Sg[x];
@@ -126,8 +117,10 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         for (int i = threadIdx.x; i < reached; i += NT) W.acc[W.qd[i]] = 0.0;
         __syncthreads();
     }
-    atomicAdd(&A.counters[0], cv);
-    atomicAdd(&A.counters[1], ce);
+    if (threadIdx.x == 0) {
+        atomicAdd(&A.counters[0], sm.walked_v);
+        atomicAdd(&A.counters[1], sm.walked_e);
+    }
 }
 
 // bc[v] = sum over roots r (in root order) of delta[r][v], skipping v == root.

@@ -71,8 +71,7 @@ struct UpdSmem {
 
 template <int NT>
 __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, const Scratch& W, int r,
-                                        int a, int b, bool moving, int g, unsigned long long& cv,
-                                        unsigned long long& ce)
+                                        int a, int b, bool moving, int g)
 {
     const int64_t nv = A.nv;
     int32_t* D = A.dist + (size_t)r * nv;
@@ -99,14 +98,9 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         const int L = Lb + step;
         const int tag = step + 2;
         lb_walk<NT>(
-            A.G, g, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
-            [&](int j, int x, int d) {
-                sm.dp[j] = W.dp[x];
-                cv++;
-                ce += (unsigned)d;
-            },
-            [&](int j, int x, int k) {
-                const int dk = D[k];
+            A.G, g, D, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
+            [&](int j, int x, int d) { sm.dp[j] = W.dp[x]; },
+            [&](int j, int x, int k, int dk) {
                 if (moving ? (dk <= L) : (dk != L + 1)) return;
                 int s = W.st[k];
                 if (s == 0) {
@@ -162,11 +156,8 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         if (x != root) atomicAdd(&A.bc[x], nD - oD);
         S[x] = nS;
         Dl[x] = nD;
-        cv++;
-        ce += (unsigned)d;
     };
-    auto parent_edge = [&](int j, int x, int k) -> bool {
-        const int dk = D[k];
+    auto parent_edge = [&](int j, int x, int k, int dk) -> bool {
         if (dk != L - 1) return false;
         const int sk = W.st[k];
         const bool kDown = (sk & SBC_STEP_MASK) != 0;
@@ -196,15 +187,15 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         }
         const int next_lo = sm.at;
         if (!moving) {
-            lb_walk<NT>(A.G, g, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,
-                        [&](int j, int x, int k) { parent_edge(j, x, k); }, NoPost());
+            lb_walk<NT>(A.G, g, D, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,
+                        [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
         } else {
             const int same_lo = sm.st;
             lb_walk<NT>(
-                A.G, g, dlist, dn, nullptr, 0, sm.lb, prep,
-                [&](int j, int x, int k) {
-                    if (parent_edge(j, x, k)) return;
-                    if (!(sm.fl[j] & 1) || D[k] != L) return;
+                A.G, g, D, dlist, dn, nullptr, 0, sm.lb, prep,
+                [&](int j, int x, int k, int dk) {
+                    if (parent_edge(j, x, k, dk)) return;
+                    if (!(sm.fl[j] & 1) || dk != L) return;
                     // k kept its level and lost the moved vertex x as a child
                     const int sk = W.st[k];
                     if (sk & SBC_STEP_MASK) return;
@@ -219,8 +210,8 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
                 },
                 NoPost());
             const int same_hi = sm.st;
-            lb_walk<NT>(A.G, g, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
-                        prep, [&](int j, int x, int k) { parent_edge(j, x, k); }, NoPost());
+            lb_walk<NT>(A.G, g, D, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
+                        prep, [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
         }
         ua_lo = next_lo;
         ua_hi = sm.at;
@@ -248,15 +239,16 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
     __syncthreads();
 }
 
-template <int NT>
-__global__ void __launch_bounds__(NT) k_update(UpdateArgs A)
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_update(UpdateArgs A)
 {
     __shared__ UpdSmem<NT> sm;
     const int64_t nv = A.nv;
     const Scratch W = A.scr.of(blockIdx.x, nv);
     const int nwork = *A.nwork;
     const int g_all = INT_MAX;
-    unsigned long long cv = 0, ce = 0, c1 = 0, c2 = 0;
+    unsigned long long c1 = 0, c2 = 0;
+    if (threadIdx.x == 0) sm.lb.walked_v = sm.lb.walked_e = 0;
 
     for (;;) {
         if (threadIdx.x == 0) sm.item = atomicAdd(A.work_counter, 1);
@@ -279,12 +271,12 @@ __global__ void __launch_bounds__(NT) k_update(UpdateArgs A)
                 if (moving) c2++;
                 else c1++;
             }
-            run_job<NT>(A, sm, W, r, a, b, moving, A.all_visible ? g_all : i, cv, ce);
+            run_job<NT>(A, sm, W, r, a, b, moving, A.all_visible ? g_all : i);
         }
     }
-    atomicAdd(&A.counters[0], cv);
-    atomicAdd(&A.counters[1], ce);
     if (threadIdx.x == 0) {
+        atomicAdd(&A.counters[0], sm.lb.walked_v);
+        atomicAdd(&A.counters[1], sm.lb.walked_e);
         atomicAdd(&A.counters[2], c1);
         atomicAdd(&A.counters[3], c2);
     }
@@ -306,14 +298,46 @@ __global__ void k_classify(const int32_t* __restrict__ dist, int64_t nv, int nk,
     }
 }
 
-constexpr int kUpdateThreads = 256;
+// Launch shapes of k_update: threads per persistent CTA and the minimum number
+// of resident CTAs per SM the compiler must fit (which caps registers).  More
+// resident CTAs means more roots in flight and more outstanding gathers; more
+// threads per CTA means faster walks over one root's frontiers.
+template <int NT, int MINB>
+void launch_variant(const UpdateArgs& A, int grid, cudaStream_t s)
+{
+    k_update<NT, MINB><<<grid, NT, 0, s>>>(A);
+}
 
-int update_workers_per_sm()
+template <int NT, int MINB>
+int occupancy_variant()
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_update<kUpdateThreads>, kUpdateThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_update<NT, MINB>, NT, 0);
     return n;
 }
+
+struct UpdateVariant {
+    int threads, min_blocks;
+    void (*launch)(const UpdateArgs&, int, cudaStream_t);
+    int (*occupancy)();
+};
+
+static const UpdateVariant kVariants[] = {
+    {256, 4, launch_variant<256, 4>, occupancy_variant<256, 4>},
+    {256, 5, launch_variant<256, 5>, occupancy_variant<256, 5>},
+    {256, 6, launch_variant<256, 6>, occupancy_variant<256, 6>},
+    {128, 8, launch_variant<128, 8>, occupancy_variant<128, 8>},
+    {128, 10, launch_variant<128, 10>, occupancy_variant<128, 10>},
+    {512, 2, launch_variant<512, 2>, occupancy_variant<512, 2>},
+};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+constexpr int kDefaultVariant = 0;
+
+int update_variant_count() { return kNumVariants; }
+int update_default_variant() { return kDefaultVariant; }
+int update_variant_threads(int v) { return kVariants[v].threads; }
+
+int update_workers_per_sm(int v) { return kVariants[v].occupancy(); }
 
 cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
 {
@@ -350,7 +374,7 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     A.counters = f->d_counters;
     const int grid = (int)std::min<int64_t>(f->workers, f->nk);
     f->prof_begin(PROF_UPDATE);
-    k_update<kUpdateThreads><<<grid, kUpdateThreads, 0, s>>>(A);
+    kVariants[f->variant].launch(A, grid, s);
     f->prof_end(PROF_UPDATE);
     return cudaGetLastError();
 }

@@ -87,6 +87,10 @@ def load(path: str = LIB_PATH):
         "sbc_graph_reserve": (C.c_int, [_vp, C.c_int64, _i64p, _i64p]),
         "sbc_graph_repacks": (C.c_int, [_vp, _i64p]),
         "sbc_forest_create": (C.c_int, [C.POINTER(_vp), _vp, C.c_int64, _i64p, C.c_int64]),
+        "sbc_forest_create_ex": (C.c_int, [C.POINTER(_vp), _vp, C.c_int64, _i64p, C.c_int64, C.c_int]),
+        "sbc_update_variant_count": (C.c_int, [C.POINTER(C.c_int)]),
+        "sbc_update_variant_info": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                              C.POINTER(C.c_int)]),
         "sbc_forest_destroy": (C.c_int, [_vp]),
         "sbc_forest_info": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p]),
         "sbc_static_init": (C.c_int, [_vp]),
@@ -182,12 +186,13 @@ class DeviceGraph:
 class DeviceForest:
     """sbc_forest: per-root dist/sigma/delta and BC on the device."""
 
-    def __init__(self, graph: DeviceGraph, roots, workers: int = 0):
+    def __init__(self, graph: DeviceGraph, roots, workers: int = 0, variant: int = -1):
         self.lib = load()
         self.graph = graph
         self.roots = _a64(roots)
         h = _vp()
-        _check(self.lib.sbc_forest_create(C.byref(h), graph.h, self.roots.size, p64(self.roots), int(workers)))
+        _check(self.lib.sbc_forest_create_ex(C.byref(h), graph.h, self.roots.size, p64(self.roots), int(workers),
+                                             int(variant)))
         self.h = h
         self.nv = graph.nv
         self.nk = int(self.roots.size)
