@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--variant", type=int, default=-1, help="update-kernel launch shape (-1 = library default)")
     p.add_argument("--workers", type=int, default=0, help="persistent workers (0 = automatic)")
+    p.add_argument("--roots", type=int, default=0,
+                   help="use only the first N roots of the workload (profiling captures; 0 = all)")
     return p.parse_args()
 
 
@@ -251,6 +253,8 @@ def run_ours(args):
     n_plain = args.plain
     t0 = time.time()
     g, roots, ins = load_workload(args.workload, n_dev + n_e2e + n_plain)
+    if args.roots:
+        roots = roots[:args.roots]
     gen_s = time.time() - t0
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
     f = native.DeviceForest(dg, roots, workers=args.workers, variant=args.variant)

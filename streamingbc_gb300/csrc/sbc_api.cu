@@ -454,14 +454,15 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     f->sm_count = prop.multiProcessorCount;
     const size_t cells = (size_t)nk * (size_t)f->nv;
     cudaError_t e;
-    if ((e = dev_alloc(&f->d_roots, nk)) || (e = dev_alloc(&f->d_dist, cells)) || (e = dev_alloc(&f->d_sigma, cells)) ||
+    if ((e = dev_alloc(&f->d_roots, nk)) || (e = dev_alloc(&f->d_dist, cells)) || (e = dev_alloc(&f->d_dist8, cells)) ||
+        (e = dev_alloc(&f->d_sigma, cells)) ||
         (e = dev_alloc(&f->d_delta, cells)) || (e = dev_alloc(&f->d_bc, f->nv)) || (e = dev_alloc(&f->d_worklist, nk)) ||
         (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, 4))) {
         sbc_forest_destroy(f);
         return cuda_fail(e, "sbc_forest_create state allocation");
     }
     f->d_counter = f->d_nwork + 1;
-    f->bytes = (int64_t)(cells * 20 + f->nv * 8);
+    f->bytes = (int64_t)(cells * 21 + f->nv * 8);
 
     // Persistent workers: as many as the update kernel keeps resident, and
     // their scratch (36 B per vertex each) limited to half of the memory still
@@ -507,6 +508,7 @@ int sbc_forest_destroy(sbc_forest* f)
     }
     dev_free(f->d_roots);
     dev_free(f->d_dist);
+    dev_free(f->d_dist8);
     dev_free(f->d_sigma);
     dev_free(f->d_delta);
     dev_free(f->d_bc);

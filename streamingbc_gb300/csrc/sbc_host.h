@@ -56,6 +56,7 @@ struct sbc_forest {
     std::vector<int64_t> h_roots;
     int64_t* d_roots = nullptr;
     int32_t* d_dist = nullptr;
+    uint8_t* d_dist8 = nullptr;  // one-byte shadow of d_dist gathered by the walkers
     int64_t* d_sigma = nullptr;
     double* d_delta = nullptr;
     double* d_bc = nullptr;

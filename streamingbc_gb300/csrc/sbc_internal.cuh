@@ -18,6 +18,13 @@
 
 #define SBC_INF 0x7fffffff
 
+// One-byte shadow of dist, gathered by the frontier walkers (dist8[K][V]):
+// 0..253 exact level, 254 = level >= 254 (read the int32 dist), 255 = unreachable.
+// A root's gathered row shrinks from 4 B to 1 B per vertex, so a hub's sorted
+// neighbour list touches fewer DRAM sectors and more of the row stays in L2.
+#define SBC_D8_DEEP 254
+#define SBC_D8_INF 255
+
 // Worker state bits (st[]).  Low bits: descent step + 1 (0 = not a descent
 // vertex).  MOVED: the vertex moved up a level.  ASC: touched by the ascent only.
 #define SBC_STEP_MASK 0x03ffffff
@@ -80,6 +87,11 @@ __device__ __forceinline__ int vis_deg(const DevGraph& G, int x, int64_t rs, int
     return d0;
 }
 
+__device__ __forceinline__ uint8_t enc_d8(int d)
+{
+    return d == SBC_INF ? (uint8_t)SBC_D8_INF : (d >= SBC_D8_DEEP ? (uint8_t)SBC_D8_DEEP : (uint8_t)d);
+}
+
 __device__ __forceinline__ void atomic_add_i64(int64_t* p, int64_t v)
 {
     atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
@@ -136,11 +148,12 @@ constexpr int kEdgeIlp = 4;
 // ranges (l1[0..n1) then l2[0..n2)).  Vertices are taken NT at a time; each
 // thread runs prep(j, x, visible_degree) for its vertex, an exclusive scan of
 // the visible degrees spreads the chunk's edges evenly over the block, and
-// edge(j, x, k, D[k]) runs once per visible neighbour k (consecutive threads
-// read consecutive adjacency slots; D is the root's distance row, gathered by
-// the walker).  post(j, x) runs after the chunk's edges.  Ends with a barrier.
+// edge(j, x, k, dist[k]) runs once per visible neighbour k (consecutive threads
+// read consecutive adjacency slots; the distance is gathered by the walker from
+// the root's one-byte row D8, falling back to the int32 row D only for levels
+// >= 254).  post(j, x) runs after the chunk's edges.  Ends with a barrier.
 template <int NT, class Prep, class Edge, class Post>
-__device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t* __restrict__ D,
+__device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t* D, const uint8_t* D8,
                                         const int32_t* l1, int n1, const int32_t* l2, int n2, LbSmem<NT>& sm,
                                         Prep prep, Edge edge, Post post)
 {
@@ -190,7 +203,12 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t*
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kEdgeIlp; ++u) dk[u] = kk[u] >= 0 ? D[kk[u]] : 0;
+            for (int u = 0; u < kEdgeIlp; ++u) dk[u] = kk[u] >= 0 ? (int)D8[kk[u]] : 0;
+#pragma unroll
+            for (int u = 0; u < kEdgeIlp; ++u) {
+                if (dk[u] == SBC_D8_INF) dk[u] = SBC_INF;
+                else if (dk[u] == SBC_D8_DEEP) dk[u] = D[kk[u]];
+            }
 #pragma unroll
             for (int u = 0; u < kEdgeIlp; ++u)
                 if (kk[u] >= 0) edge(jj[u], sm.x[jj[u]], kk[u], dk[u]);

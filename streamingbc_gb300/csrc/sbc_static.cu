@@ -24,6 +24,7 @@ struct StaticArgs {
     int nk;
     const int64_t* roots;
     int32_t* dist;
+    uint8_t* dist8;
     int64_t* sigma;
     double* delta;
     ScratchBase scr;
@@ -49,18 +50,21 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         __syncthreads();
         if (r >= A.nk) break;
         int32_t* D = A.dist + (size_t)r * nv;
+        uint8_t* D8 = A.dist8 + (size_t)r * nv;
         int64_t* Sg = A.sigma + (size_t)r * nv;
         double* Dl = A.delta + (size_t)r * nv;
         const int root = (int)A.roots[r];
 
         for (int64_t x = threadIdx.x; x < nv; x += NT) {
             D[x] = SBC_INF;
+            D8[x] = SBC_D8_INF;
             Sg[x] = 0;
             Dl[x] = 0.0;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             D[root] = 0;
+            D8[root] = 0;
             Sg[root] = 1;
             W.qd[0] = root;
             W.lvl[0] = 0;
@@ -73,12 +77,13 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         int L = 0, lo = 0, hi = 1;
         while (lo < hi) {
             lb_walk<NT>(
-                A.G, INT_MAX, D, W.qd + lo, hi - lo, nullptr, 0, sm,
+                A.G, INT_MAX, D, D8, W.qd + lo, hi - lo, nullptr, 0, sm,
                 [&](int j, int x, int d) { s_sig[j] = Sg[x]; },
                 [&](int j, int x, int k, int dk) {
                     if (dk == SBC_INF) {
                         int old = atomicCAS(&D[k], SBC_INF, L + 1);
                         if (old == SBC_INF) {
+                            D8[k] = enc_d8(L + 1);
                             int p = atomicAdd(&s_tail, 1);
                             W.qd[p] = k;
                             dk = L + 1;
@@ -101,7 +106,7 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         for (int l = nlev - 1; l >= 0; --l) {
             const int b0 = W.lvl[l], b1 = W.lvl[l + 1];
             lb_walk<NT>(
-                A.G, INT_MAX, D, W.qd + b0, b1 - b0, nullptr, 0, sm,
+                A.G, INT_MAX, D, D8, W.qd + b0, b1 - b0, nullptr, 0, sm,
                 [&](int j, int x, int d) { s_acc[j] = 0.0; },
                 [&](int j, int x, int k, int dk) {
                     if (dk == l + 1) atomicAdd(&s_acc[j], W.acc[k]);
@@ -138,12 +143,10 @@ __global__ void k_bc_colsum(const double* __restrict__ delta, const int64_t* __r
     }
 }
 
-constexpr int kStaticThreads = 256;
-
 int static_workers_per_sm()
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_static<kStaticThreads>, kStaticThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_static<256>, 256, 0);
     return n;
 }
 
@@ -159,14 +162,19 @@ cudaError_t launch_static(sbc_forest* f)
     A.nk = (int)f->nk;
     A.roots = f->d_roots;
     A.dist = f->d_dist;
+    A.dist8 = f->d_dist8;
     A.sigma = f->d_sigma;
     A.delta = f->d_delta;
     A.scr = f->scratch();
     A.work_counter = f->d_counter;
     A.counters = f->d_counters;
-    int grid = (int)std::min<int64_t>(f->workers, f->nk);
+    // One worker slot per CTA: with few workers per SM, wider CTAs keep the SMs full.
+    const int grid = (int)std::min<int64_t>(f->workers, f->nk);
+    const int64_t per_sm = (f->workers + f->sm_count - 1) / f->sm_count;
     f->prof_begin(PROF_STATIC);
-    k_static<kStaticThreads><<<grid, kStaticThreads, 0, s>>>(A);
+    if (per_sm <= 1) k_static<1024><<<grid, 1024, 0, s>>>(A);
+    else if (per_sm <= 2) k_static<512><<<grid, 512, 0, s>>>(A);
+    else k_static<256><<<grid, 256, 0, s>>>(A);
     f->prof_end(PROF_STATIC);
     if ((e = cudaGetLastError())) return e;
     int bgrid = (int)std::min<int64_t>((f->nv + 255) / 256, (int64_t)f->sm_count * 8);

@@ -44,6 +44,7 @@ struct UpdateArgs {
     int nk;
     const int64_t* roots;
     int32_t* dist;
+    uint8_t* dist8;
     int64_t* sigma;
     double* delta;
     double* bc;
@@ -75,6 +76,7 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
 {
     const int64_t nv = A.nv;
     int32_t* D = A.dist + (size_t)r * nv;
+    uint8_t* D8 = A.dist8 + (size_t)r * nv;
     int64_t* S = A.sigma + (size_t)r * nv;
     double* Dl = A.delta + (size_t)r * nv;
     const int root = (int)A.roots[r];
@@ -98,7 +100,7 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         const int L = Lb + step;
         const int tag = step + 2;
         lb_walk<NT>(
-            A.G, g, D, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
+            A.G, g, D, D8, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
             [&](int j, int x, int d) { sm.dp[j] = W.dp[x]; },
             [&](int j, int x, int k, int dk) {
                 if (moving ? (dk <= L) : (dk != L + 1)) return;
@@ -133,6 +135,7 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
             const int nl = Lb + (s & SBC_STEP_MASK) - 1;
             if (D[k] != nl) {
                 D[k] = nl;
+                D8[k] = enc_d8(nl);
                 W.st[k] = s | SBC_MOVED;
             }
         }
@@ -187,12 +190,12 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         }
         const int next_lo = sm.at;
         if (!moving) {
-            lb_walk<NT>(A.G, g, D, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,
+            lb_walk<NT>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,
                         [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
         } else {
             const int same_lo = sm.st;
             lb_walk<NT>(
-                A.G, g, D, dlist, dn, nullptr, 0, sm.lb, prep,
+                A.G, g, D, D8, dlist, dn, nullptr, 0, sm.lb, prep,
                 [&](int j, int x, int k, int dk) {
                     if (parent_edge(j, x, k, dk)) return;
                     if (!(sm.fl[j] & 1) || dk != L) return;
@@ -210,7 +213,7 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
                 },
                 NoPost());
             const int same_hi = sm.st;
-            lb_walk<NT>(A.G, g, D, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
+            lb_walk<NT>(A.G, g, D, D8, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
                         prep, [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
         }
         ua_lo = next_lo;
@@ -329,9 +332,16 @@ static const UpdateVariant kVariants[] = {
     {128, 8, launch_variant<128, 8>, occupancy_variant<128, 8>},
     {128, 10, launch_variant<128, 10>, occupancy_variant<128, 10>},
     {512, 2, launch_variant<512, 2>, occupancy_variant<512, 2>},
+    {512, 1, launch_variant<512, 1>, occupancy_variant<512, 1>},
+    {1024, 1, launch_variant<1024, 1>, occupancy_variant<1024, 1>},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
-constexpr int kDefaultVariant = 0;
+// 1024 threads x 1 CTA per SM measured fastest on R-MAT scale 20, K = 1024
+// (531 insertions/s against 413 for 512x2 and 281 for 256x4): with one root in
+// flight per SM, the in-flight one-byte distance rows (152 x 1 MB) about fit
+// the 129 MB L2, so repeated scans of the same hub ancestors within a root's
+// batch hit L2 instead of HBM.
+constexpr int kDefaultVariant = 7;
 
 int update_variant_count() { return kNumVariants; }
 int update_default_variant() { return kDefaultVariant; }
@@ -359,6 +369,7 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     A.nk = (int)f->nk;
     A.roots = f->d_roots;
     A.dist = f->d_dist;
+    A.dist8 = f->d_dist8;
     A.sigma = f->d_sigma;
     A.delta = f->d_delta;
     A.bc = f->d_bc;

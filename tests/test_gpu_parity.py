@@ -75,6 +75,43 @@ def test_batched_insertions_match_reference(sbc_lib, case, batch):
     dg.close()
 
 
+def test_every_launch_shape_same_result(sbc_lib):
+    """Results do not depend on the update kernel's launch shape."""
+    import ctypes
+    n = ctypes.c_int()
+    assert sbc_lib.sbc_update_variant_count(ctypes.byref(n)) == 0 and n.value >= 1
+    z = load_golden("rmat9")
+    for v in range(n.value):
+        dg = native.DeviceGraph(int(z["nv"]), z["off"], z["adj"])
+        f = native.DeviceForest(dg, z["roots"], variant=v)
+        f.static_init()
+        for s in range(0, len(z["ins"]), 16):
+            f.insert(z["ins"][s:s + 16])
+        check_state(f, z["level1"], z["sigma1"], z["bc1"])
+        f.close()
+        dg.close()
+
+
+def test_deep_levels_use_exact_fallback(sbc_lib, port_lib):
+    """A 600-vertex path: levels >= 254 do not fit the one-byte distance shadow
+    and must be read from the int32 distances; shortcuts then move long
+    stretches up by hundreds of levels."""
+    n = 600
+    a = np.arange(n - 1)
+    g = G.from_edges(n, a, a + 1)
+    roots = np.array([0, 1, 299, 599], dtype=np.int64)
+    ins = np.array([(0, 400), (100, 550), (250, 260), (5, 590), (300, 310), (0, 599)], dtype=np.int64)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots, nthreads=2)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    check_state(f, o.level(), o.sigma(), o.bc())
+    for u, v in ins:
+        o.insert(int(u), int(v))
+        f.insert([(u, v)])
+        check_state(f, o.level(), o.sigma(), o.bc())
+
+
 @pytest.mark.parametrize("workers", [1, 3])
 def test_few_workers_same_result(sbc_lib, workers):
     z = load_golden("rmat9")
