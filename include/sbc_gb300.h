@@ -50,6 +50,8 @@ typedef struct {
     int64_t case2;        /* (insertion, root) pairs with |d| > 1 */
     int64_t vertices;     /* traversed vertices */
     int64_t edges;        /* traversed edges (sum of degrees of traversed vertices) */
+    int64_t scanned;      /* adjacency slots the kernels actually scanned (fewer than
+                             `edges` where parents were found from the parent side) */
 } sbc_batch_stats;
 
 /* Device time per kernel kind, accumulated while profiling is on. */
@@ -139,8 +141,10 @@ int sbc_update_inserted(sbc_forest *f, int64_t n, const int64_t *u, const int64_
 
 /* Wait for all work queued on the forest's graph stream. */
 int sbc_sync(sbc_forest *f);
-/* Read and reset the traversal/case counters accumulated since the last read. */
-int sbc_read_counters(sbc_forest *f, int64_t *vertices, int64_t *edges, int64_t *case1, int64_t *case2);
+/* Read and reset the traversal/case counters accumulated since the last read
+ * (any pointer may be NULL); `scanned` is the adjacency slots actually read. */
+int sbc_read_counters(sbc_forest *f, int64_t *vertices, int64_t *edges, int64_t *case1, int64_t *case2,
+                      int64_t *scanned);
 
 /* ---- state read-back (synchronous) ------------------------------------- */
 

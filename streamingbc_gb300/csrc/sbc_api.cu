@@ -191,7 +191,7 @@ int collect_stats(sbc_forest* f, int64_t n, sbc_batch_stats* st)
                               g->stream));
     int nwork = 0;
     CK(cudaMemcpyAsync(&nwork, f->d_nwork, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
-    unsigned long long c[4];
+    unsigned long long c[SBC_NCOUNTERS];
     CK(cudaMemcpyAsync(c, f->d_counters, sizeof c, cudaMemcpyDeviceToHost, g->stream));
     CK(cudaMemsetAsync(f->d_counters, 0, sizeof c, g->stream));
     CK(cudaStreamSynchronize(g->stream));
@@ -206,6 +206,7 @@ int collect_stats(sbc_forest* f, int64_t n, sbc_batch_stats* st)
     st->edges = (int64_t)c[1];
     st->case1 = (int64_t)c[2];
     st->case2 = (int64_t)c[3];
+    st->scanned = (int64_t)c[4];
     return SBC_OK;
 }
 
@@ -457,7 +458,7 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     if ((e = dev_alloc(&f->d_roots, nk)) || (e = dev_alloc(&f->d_dist, cells)) || (e = dev_alloc(&f->d_dist8, cells)) ||
         (e = dev_alloc(&f->d_sigma, cells)) ||
         (e = dev_alloc(&f->d_delta, cells)) || (e = dev_alloc(&f->d_bc, f->nv)) || (e = dev_alloc(&f->d_worklist, nk)) ||
-        (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, 4))) {
+        (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, SBC_NCOUNTERS))) {
         sbc_forest_destroy(f);
         return cuda_fail(e, "sbc_forest_create state allocation");
     }
@@ -489,7 +490,7 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     CK(cudaMemsetAsync(f->d_st, 0, sizeof(int32_t) * sc, g->stream));
     CK(cudaMemsetAsync(f->d_dp, 0, sizeof(int64_t) * sc, g->stream));
     CK(cudaMemsetAsync(f->d_acc, 0, sizeof(double) * sc, g->stream));
-    CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * 4, g->stream));
+    CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
     CK(cudaMemcpyAsync(f->d_roots, roots, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, g->stream));
     CK(f->prof_init());
     CK(cudaEventCreate(&f->t0));
@@ -563,7 +564,7 @@ int sbc_insert_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* 
     if (rc) return rc;
     if ((rc = stage_host(g, n, u, v, false))) return rc;
     // per-call statistics cover this call only
-    if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * 4, g->stream));
+    if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
     f->prof_begin(sbc::PROF_BATCH);
     f->prof_begin(sbc::PROF_APPEND);
     CK(sbc::launch_append(g, (int)n, false));
@@ -610,7 +611,7 @@ int sbc_update_inserted(sbc_forest* f, int64_t n, const int64_t* u, const int64_
     }
     int rc = stage_host(g, n, u, v, true);
     if (rc) return rc;
-    if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * 4, g->stream));
+    if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
     f->prof_begin(sbc::PROF_BATCH);
     CK(sbc::launch_update(f, (int)n, true));
     f->prof_end(sbc::PROF_BATCH);
@@ -627,11 +628,12 @@ int sbc_sync(sbc_forest* f)
     return check_graph_err(f->g);
 }
 
-int sbc_read_counters(sbc_forest* f, int64_t* vertices, int64_t* edges, int64_t* case1, int64_t* case2)
+int sbc_read_counters(sbc_forest* f, int64_t* vertices, int64_t* edges, int64_t* case1, int64_t* case2,
+                      int64_t* scanned)
 {
     if (!f) return fail(SBC_ERR_ARG, "sbc_read_counters: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
-    unsigned long long c[4];
+    unsigned long long c[SBC_NCOUNTERS];
     CK(cudaMemcpyAsync(c, f->d_counters, sizeof c, cudaMemcpyDeviceToHost, f->g->stream));
     CK(cudaMemsetAsync(f->d_counters, 0, sizeof c, f->g->stream));
     CK(cudaStreamSynchronize(f->g->stream));
@@ -639,6 +641,7 @@ int sbc_read_counters(sbc_forest* f, int64_t* vertices, int64_t* edges, int64_t*
     if (edges) *edges = (int64_t)c[1];
     if (case1) *case1 = (int64_t)c[2];
     if (case2) *case2 = (int64_t)c[3];
+    if (scanned) *scanned = (int64_t)c[4];
     return SBC_OK;
 }
 
@@ -895,7 +898,7 @@ static void static_common(bcForest* forest, struct stinger* G, extraArraysPerThr
     if (!forest->sbc && sbc_forest_create(&forest->sbc, G->g, forest->sbc_nk, forest->sbc_roots, 0)) return;
     if (sbc_static_init(forest->sbc)) return;
     int64_t vtx = 0, edg = 0;
-    if (sbc_read_counters(forest->sbc, &vtx, &edg, nullptr, nullptr)) return;
+    if (sbc_read_counters(forest->sbc, &vtx, &edg, nullptr, nullptr, nullptr)) return;
     if (aux && aux[0]) {
         aux[0]->staticTraverseVerticeCounter += vtx;
         aux[0]->staticTraverseEdgeCounter += edg;

@@ -6,6 +6,8 @@
 #include <vector>
 #include "sbc_internal.cuh"
 
+#define SBC_NCOUNTERS 5
+
 namespace sbc {
 
 enum ProfKernel { PROF_STATIC = 0, PROF_APPEND, PROF_CLASSIFY, PROF_UPDATE, PROF_BATCH, PROF_COUNT };
@@ -75,7 +77,9 @@ struct sbc_forest {
     int* d_worklist = nullptr;
     int* d_nwork = nullptr;   // [1]
     int* d_counter = nullptr; // [1]
-    unsigned long long* d_counters = nullptr;  // [4]: vertices, edges, case1, case2
+    // [SBC_NCOUNTERS]: traversed vertices, traversed edges (reference counters),
+    // case-1 pairs, case-2 pairs, adjacency slots actually scanned
+    unsigned long long* d_counters = nullptr;
     int64_t bytes = 0;
     // profiling: a ring of CUDA event pairs per kernel kind; pairs are read
     // back only when the ring wraps or the profile is queried, so recording

@@ -134,8 +134,9 @@ struct LbSmem {
     int off[NT + 1];
     int64_t row[NT];
     int warp[NT / 32];
-    // traversal counters of the block: vertices walked and their visible degrees
-    unsigned long long walked_v, walked_e;
+    // traversal counters of the block: vertices walked and their visible
+    // degrees as the reference counts them, and adjacency slots actually scanned
+    unsigned long long walked_v, walked_e, scanned_e;
 };
 
 // Edges each thread has in flight per round of the walker: the adjacency
@@ -152,7 +153,9 @@ constexpr int kEdgeIlp = 4;
 // read consecutive adjacency slots; the distance is gathered by the walker from
 // the root's one-byte row D8, falling back to the int32 row D only for levels
 // >= 254).  post(j, x) runs after the chunk's edges.  Ends with a barrier.
-template <int NT, class Prep, class Edge, class Post>
+// REF: the walked vertices and their degrees count as traversed in the
+// reference's sense (COUNT_TRAVERSALS); every walk counts its scanned slots.
+template <int NT, bool REF = true, class Prep, class Edge, class Post>
 __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t* D, const uint8_t* D8,
                                         const int32_t* l1, int n1, const int32_t* l2, int n2, LbSmem<NT>& sm,
                                         Prep prep, Edge edge, Post post)
@@ -176,8 +179,11 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t*
         if (t < cnt) sm.off[t] = off;
         if (t == 0) {
             sm.off[cnt] = total;
-            sm.walked_v += (unsigned)cnt;
-            sm.walked_e += (unsigned)total;
+            if (REF) {
+                sm.walked_v += (unsigned)cnt;
+                sm.walked_e += (unsigned)total;
+            }
+            sm.scanned_e += (unsigned)total;
         }
         __syncthreads();
         int j = 0;  // chunk vertex of this thread's current edge; edges only move forward
@@ -222,5 +228,21 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t*
 struct NoPost {
     __device__ void operator()(int, int) const {}
 };
+
+// Block-wide sum of one 64-bit value per thread (all threads get the total).
+template <int NT>
+__device__ __forceinline__ long long block_sum(long long v, long long* s_part)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_part[wid] = v;
+    __syncthreads();
+    long long t = 0;
+#pragma unroll 4
+    for (int w = 0; w < NT / 32; ++w) t += s_part[w];
+    __syncthreads();
+    return t;
+}
 
 }  // namespace sbc

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
     __shared__ double s_acc[NT];
     const int64_t nv = A.nv;
     Scratch W = A.scr.of(blockIdx.x, nv);
-    if (threadIdx.x == 0) sm.walked_v = sm.walked_e = 0;
+    if (threadIdx.x == 0) sm.walked_v = sm.walked_e = sm.scanned_e = 0;
 
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(A.work_counter, 1);
@@ -125,6 +125,7 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
     if (threadIdx.x == 0) {
         atomicAdd(&A.counters[0], sm.walked_v);
         atomicAdd(&A.counters[1], sm.walked_e);
+        atomicAdd(&A.counters[4], sm.scanned_e);
     }
 }
 

@@ -57,7 +57,7 @@ struct UpdateArgs {
     const int* worklist;
     const int* nwork;
     int* work_counter;
-    unsigned long long* counters;  // vertices, edges, case1, case2
+    unsigned long long* counters;  // vertices, edges, case1, case2, scanned
 };
 
 template <int NT>
@@ -67,7 +67,9 @@ struct UpdSmem {
     double wn[NT];
     double wo[NT];
     int fl[NT];
+    long long part[NT / 32];
     int item, qt, at, st;
+    int root_slot;  // the root's id, as a one-element vertex list
 };
 
 template <int NT>
@@ -144,7 +146,10 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
 
     // ---------------- ascent ----------------
     int L = 0;
-    auto prep = [&](int j, int x, int d) {
+    // Finalise vertex x of the level being walked: new sigma/delta committed in
+    // place, BC += newdelta - olddelta, and its push weights returned:
+    // wn = (newdelta+1)/newsigma, wo = (olddelta+1)/oldsigma.
+    auto commit = [&](int x, double& wn, double& wo) {
         const int s = W.st[x];
         const bool isDown = (s & SBC_STEP_MASK) != 0;
         const bool mv = (s & SBC_MOVED) != 0;
@@ -153,12 +158,24 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         const double ac = W.acc[x];
         const int64_t nS = isDown ? (mv ? W.dp[x] : oS + W.dp[x]) : oS;
         const double nD = isDown ? ac : oD + ac;
-        sm.wn[j] = (nD + 1.0) / (double)nS;
-        sm.wo[j] = oS ? (oD + 1.0) / (double)oS : 0.0;
-        sm.fl[j] = (mv ? 1 : 0) | (x == b ? 2 : 0);
+        wn = (nD + 1.0) / (double)nS;
+        wo = oS ? (oD + 1.0) / (double)oS : 0.0;
         if (x != root) atomicAdd(&A.bc[x], nD - oD);
         S[x] = nS;
         Dl[x] = nD;
+    };
+    auto prep = [&](int j, int x, int d) {
+        double wn, wo;
+        commit(x, wn, wo);
+        sm.wn[j] = wn;
+        sm.wo[j] = wo;
+        sm.fl[j] = ((W.st[x] & SBC_MOVED) ? 1 : 0) | (x == b ? 2 : 0);
+    };
+    // Push weights of an already committed vertex, kept in its acc/dp slots.
+    auto prep_loaded = [&](int j, int x, int d) {
+        sm.wn[j] = W.acc[x];
+        sm.wo[j] = __longlong_as_double((long long)W.dp[x]);
+        sm.fl[j] = ((W.st[x] & SBC_MOVED) ? 1 : 0) | (x == b ? 2 : 0);
     };
     auto parent_edge = [&](int j, int x, int k, int dk) -> bool {
         if (dk != L - 1) return false;
@@ -178,6 +195,52 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         return true;
     };
 
+    // Pull form for levels 1 and 2.  The parents of a level-1 vertex can only
+    // be the root, and those of a level-2 vertex only the root's neighbours, so
+    // instead of every walked vertex scanning its (often hub-sized) adjacency
+    // for parents, each candidate parent y can scan its own adjacency for
+    // walked children c (dist = L and touched) and sum the same contributions
+    // newsigma[y]*wn[c] - [y ascent-only, (y,c) != (a,b)] sigma[y]*wo[c].  The
+    // cheaper direction is chosen per level by scanned-slot count; results are
+    // the same either way.  Used only where no vertex of the level moved (no
+    // same-level ex-parent rule applies).
+    auto pull_walk = [&](const int32_t* plist, int pn) {
+        lb_walk<NT, false>(
+            A.G, g, D, D8, plist, pn, nullptr, 0, sm.lb,
+            [&](int j, int y, int d) {
+                const int sy = W.st[y];
+                const bool yDown = (sy & SBC_STEP_MASK) != 0;
+                const int64_t oS = S[y];
+                sm.dp[j] = yDown ? ((sy & SBC_MOVED) ? W.dp[y] : oS + W.dp[y]) : oS;
+                sm.wo[j] = (double)oS;
+                sm.wn[j] = 0.0;
+                sm.fl[j] = (yDown ? 1 : 0) | (y == a ? 2 : 0);
+            },
+            [&](int j, int y, int c, int dc) {
+                if (dc != L || W.st[c] == 0) return;
+                const double wn = W.acc[c];
+                const double wo = __longlong_as_double((long long)W.dp[c]);
+                double v = (double)sm.dp[j] * wn;
+                const int fl = sm.fl[j];
+                if (!(fl & 1) && !((fl & 2) && c == b)) v -= sm.wo[j] * wo;
+                atomicAdd(&sm.wn[j], v);
+                if (!(fl & 4)) atomicOr(&sm.fl[j], 4);
+            },
+            [&](int j, int y) {
+                const int fl = sm.fl[j];
+                if (!(fl & 4)) return;
+                W.acc[y] += sm.wn[j];  // y's only contributions at this level come from this walk
+                if (!(fl & 1)) {
+                    int old = atomicOr(&W.st[y], SBC_ASC);
+                    if (!(old & SBC_ASC)) {
+                        int p = atomicAdd(&sm.at, 1);
+                        W.qa[p] = y;
+                    }
+                }
+            });
+    };
+    long long pull2_cost = -1;  // scanned slots of a level-2 pull (root's neighbours), computed once
+
     int ua_lo = 0, ua_hi = 0;
     const int Lmax = Lb + nsteps - 1;
     for (L = Lmax; L >= 0; --L) {
@@ -189,7 +252,53 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
             dn = W.lvl[ds + 1] - W.lvl[ds];
         }
         const int next_lo = sm.at;
-        if (!moving) {
+        const bool pull_ok = L >= 1 && L <= 2 && (!moving || L < Lb);
+        if (pull_ok) {
+            // Commit every vertex of the level; keep its push weights in acc/dp;
+            // count it as traversed (reference counters) and sum its degree.
+            const int na_ = ua_hi - ua_lo;
+            long long push_cost = 0;
+            for (int i = threadIdx.x; i < dn + na_; i += NT) {
+                const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
+                double wn, wo;
+                commit(x, wn, wo);
+                W.acc[x] = wn;
+                W.dp[x] = (int64_t)__double_as_longlong(wo);
+                push_cost += vis_deg(A.G, x, A.G.row[x], g);
+            }
+            push_cost = block_sum<NT>(push_cost, sm.part);
+            long long pull_cost = 0;
+            const int64_t rrow = A.G.row[root];
+            const int rdeg = vis_deg(A.G, root, rrow, g);
+            if (dn + na_ == 0) {
+                pull_cost = 1;  // nothing to walk at this level; the (empty) push walk is a no-op
+            } else if (L == 1) {
+                pull_cost = rdeg;
+            } else {
+                if (pull2_cost < 0) {
+                    long long c = 0;
+                    for (int i = threadIdx.x; i < rdeg; i += NT) {
+                        const int y = A.G.col[rrow + i];
+                        c += vis_deg(A.G, y, A.G.row[y], g);
+                    }
+                    pull2_cost = block_sum<NT>(c, sm.part);
+                }
+                pull_cost = pull2_cost;
+            }
+            if (threadIdx.x == 0) {
+                sm.lb.walked_v += (unsigned)(dn + na_);
+                sm.lb.walked_e += (unsigned long long)push_cost;
+                sm.root_slot = root;
+            }
+            __syncthreads();
+            if (pull_cost < push_cost) {
+                if (L == 1) pull_walk(&sm.root_slot, 1);
+                else pull_walk(A.G.col + rrow, rdeg);
+            } else {
+                lb_walk<NT, false>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, na_, sm.lb, prep_loaded,
+                                   [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+            }
+        } else if (!moving) {
             lb_walk<NT>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,
                         [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
         } else {
@@ -232,6 +341,7 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
     for (int i = threadIdx.x; i < na; i += NT) {
         const int k = W.qa[i];
         W.st[k] = 0;
+        W.dp[k] = 0;  // may hold a push weight (pull-form levels)
         W.acc[k] = 0.0;
     }
     for (int i = threadIdx.x; i < ns; i += NT) {
@@ -251,7 +361,7 @@ __global__ void __launch_bounds__(NT, MINB) k_update(UpdateArgs A)
     const int nwork = *A.nwork;
     const int g_all = INT_MAX;
     unsigned long long c1 = 0, c2 = 0;
-    if (threadIdx.x == 0) sm.lb.walked_v = sm.lb.walked_e = 0;
+    if (threadIdx.x == 0) sm.lb.walked_v = sm.lb.walked_e = sm.lb.scanned_e = 0;
 
     for (;;) {
         if (threadIdx.x == 0) sm.item = atomicAdd(A.work_counter, 1);
@@ -282,6 +392,7 @@ __global__ void __launch_bounds__(NT, MINB) k_update(UpdateArgs A)
         atomicAdd(&A.counters[1], sm.lb.walked_e);
         atomicAdd(&A.counters[2], c1);
         atomicAdd(&A.counters[3], c2);
+        atomicAdd(&A.counters[4], sm.lb.scanned_e);
     }
 }
 

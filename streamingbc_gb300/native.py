@@ -30,7 +30,7 @@ class SbcError(RuntimeError):
 
 class BatchStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("inserted", "duplicates", "invalid", "roots_active", "case1", "case2",
-                                          "vertices", "edges")]
+                                          "vertices", "edges", "scanned")]
 
     def as_dict(self) -> dict:
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -98,7 +98,7 @@ def load(path: str = LIB_PATH):
         "sbc_insert_batch_device": (C.c_int, [_vp, C.c_int64, _vp, _vp]),
         "sbc_update_inserted": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
         "sbc_sync": (C.c_int, [_vp]),
-        "sbc_read_counters": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p]),
+        "sbc_read_counters": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
         "sbc_get_bc": (C.c_int, [_vp, _f64p]),
         "sbc_get_dist": (C.c_int, [_vp, C.c_int64, C.c_int64, _i32p]),
         "sbc_get_sigma": (C.c_int, [_vp, C.c_int64, C.c_int64, _i64p]),
@@ -231,9 +231,10 @@ class DeviceForest:
         _check(self.lib.sbc_sync(self.h))
 
     def counters(self) -> dict:
-        v = [C.c_int64() for _ in range(4)]
+        v = [C.c_int64() for _ in range(5)]
         _check(self.lib.sbc_read_counters(self.h, *[C.byref(x) for x in v]))
-        return {"vertices": v[0].value, "edges": v[1].value, "case1": v[2].value, "case2": v[3].value}
+        return {"vertices": v[0].value, "edges": v[1].value, "case1": v[2].value, "case2": v[3].value,
+                "scanned": v[4].value}
 
     def bc(self) -> np.ndarray:
         out = np.zeros(self.nv, dtype=np.float64)
