@@ -8,8 +8,8 @@
 #include <unordered_map>
 #include <vector>
 
-#include "../../include/sbc_gb300.h"
-#include "../../include/streamingbc.h"
+#include "sbc_gb300.h"
+#include "streamingbc.h"
 #include "sbc_host.h"
 
 namespace {
@@ -285,13 +285,19 @@ int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int6
     }
     g->h_row[nv] = total;
     g->total_cap = total;
+    // Each vertex's initial neighbours are stored sorted, so adjacency can be
+    // tested by binary search (insertions later append an unsorted tail).
     std::vector<int32_t> col(total > 0 ? total : 1, 0);
-    for (int64_t v = 0; v < nv; ++v)
-        for (int64_t e = off[v]; e < off[v + 1]; ++e) col[g->h_row[v] + (e - off[v])] = (int32_t)adj[e];
+    for (int64_t v = 0; v < nv; ++v) {
+        int32_t* dst = col.data() + g->h_row[v];
+        for (int64_t e = off[v]; e < off[v + 1]; ++e) dst[e - off[v]] = (int32_t)adj[e];
+        std::sort(dst, dst + (off[v + 1] - off[v]));
+    }
 
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) || (e = dev_alloc(&g->d_row, nv + 1)) ||
         (e = dev_alloc(&g->d_deg, nv)) || (e = dev_alloc(&g->d_deg0, nv)) || (e = dev_alloc(&g->d_cap, nv)) ||
+        (e = dev_alloc(&g->d_nsort, nv)) ||
         (e = dev_alloc(&g->d_col, total)) || (e = dev_alloc(&g->d_seq, total)) || (e = dev_alloc(&g->d_err, 1))) {
         sbc_graph_destroy(g);
         return cuda_fail(e, "sbc_graph_create allocation");
@@ -299,6 +305,7 @@ int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int6
     if ((e = cudaMemcpy(g->d_row, g->h_row.data(), sizeof(int64_t) * (nv + 1), cudaMemcpyHostToDevice)) ||
         (nv && (e = cudaMemcpy(g->d_deg, deg.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
         (nv && (e = cudaMemcpy(g->d_deg0, deg.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
+        (nv && (e = cudaMemcpy(g->d_nsort, deg.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
         (nv && (e = cudaMemcpy(g->d_cap, g->h_cap.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
         (e = cudaMemcpy(g->d_col, col.data(), sizeof(int32_t) * col.size(), cudaMemcpyHostToDevice)) ||
         (e = cudaMemset(g->d_seq, 0, sizeof(int32_t) * col.size())) || (e = cudaMemset(g->d_err, 0, sizeof(int)))) {
@@ -322,6 +329,7 @@ int sbc_graph_destroy(sbc_graph* g)
     dev_free(g->d_row);
     dev_free(g->d_deg);
     dev_free(g->d_deg0);
+    dev_free(g->d_nsort);
     dev_free(g->d_cap);
     dev_free(g->d_col);
     dev_free(g->d_seq);
@@ -466,12 +474,13 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     f->bytes = (int64_t)(cells * 21 + f->nv * 8);
 
     // Persistent workers: as many as the update kernel keeps resident, and
-    // their scratch (36 B per vertex each) limited to half of the memory still
-    // free.  The static kernel runs over the same worker slots.
+    // their scratch (36 B + 1 bit per vertex each) limited to half of the
+    // memory still free.  The static kernel runs over the same worker slots.
     int per_sm = sbc::update_workers_per_sm(variant);
     if (per_sm < 1) per_sm = 1;
     int64_t w = workers > 0 ? workers : (int64_t)per_sm * f->sm_count;
-    const size_t per_worker = (size_t)f->nv * 36 + 16;
+    const size_t words = sbc::bitmap_words(f->nv);
+    const size_t per_worker = (size_t)f->nv * 36 + words * 4 + 16;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     int64_t fit = (int64_t)((free_b / 2) / per_worker);
@@ -482,11 +491,13 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     const size_t sc = (size_t)w * (size_t)f->nv;
     if ((e = dev_alloc(&f->d_st, sc)) || (e = dev_alloc(&f->d_dp, sc)) || (e = dev_alloc(&f->d_acc, sc)) ||
         (e = dev_alloc(&f->d_qd, sc)) || (e = dev_alloc(&f->d_qa, sc)) || (e = dev_alloc(&f->d_qs, sc)) ||
-        (e = dev_alloc(&f->d_lvl, (size_t)w * (size_t)(f->nv + 2)))) {
+        (e = dev_alloc(&f->d_lvl, (size_t)w * (size_t)(f->nv + 2))) ||
+        (e = dev_alloc(&f->d_bits, (size_t)w * words))) {
         sbc_forest_destroy(f);
         return cuda_fail(e, "sbc_forest_create scratch allocation");
     }
-    f->bytes += (int64_t)(sc * 36);
+    f->bytes += (int64_t)(sc * 36 + (size_t)w * words * 4);
+    CK(cudaMemsetAsync(f->d_bits, 0, sizeof(uint32_t) * (size_t)w * words, g->stream));
     CK(cudaMemsetAsync(f->d_st, 0, sizeof(int32_t) * sc, g->stream));
     CK(cudaMemsetAsync(f->d_dp, 0, sizeof(int64_t) * sc, g->stream));
     CK(cudaMemsetAsync(f->d_acc, 0, sizeof(double) * sc, g->stream));
@@ -523,6 +534,7 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_qa);
     dev_free(f->d_qs);
     dev_free(f->d_lvl);
+    dev_free(f->d_bits);
     f->prof_release();
     if (f->t0) cudaEventDestroy(f->t0);
     if (f->t1) cudaEventDestroy(f->t1);

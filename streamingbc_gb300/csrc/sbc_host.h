@@ -25,6 +25,7 @@ struct sbc_graph {
     int64_t* d_row = nullptr;
     int32_t* d_deg = nullptr;
     int32_t* d_deg0 = nullptr;
+    int32_t* d_nsort = nullptr;  // leading slots of each vertex stored in sorted order
     int32_t* d_cap = nullptr;
     int32_t* d_col = nullptr;
     int32_t* d_seq = nullptr;
@@ -46,6 +47,7 @@ struct sbc_graph {
         G.row = d_row;
         G.deg = d_deg;
         G.deg0 = d_deg0;
+        G.nsort = d_nsort;
         G.col = d_col;
         G.seq = d_seq;
         return G;
@@ -74,6 +76,7 @@ struct sbc_forest {
     int32_t* d_qa = nullptr;
     int32_t* d_qs = nullptr;
     int32_t* d_lvl = nullptr;
+    uint32_t* d_bits = nullptr;
     int* d_worklist = nullptr;
     int* d_nwork = nullptr;   // [1]
     int* d_counter = nullptr; // [1]
@@ -104,6 +107,7 @@ struct sbc_forest {
         s.qa = d_qa;
         s.qs = d_qs;
         s.lvl = d_lvl;
+        s.bits = d_bits;
         return s;
     }
     cudaError_t prof_init()

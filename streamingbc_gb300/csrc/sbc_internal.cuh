@@ -38,6 +38,7 @@ struct DevGraph {
     const int64_t* row;
     const int32_t* deg;
     const int32_t* deg0;
+    const int32_t* nsort;  // the first nsort[v] slots of v are sorted by neighbour id
     const int32_t* col;
     const int32_t* seq;
 };
@@ -50,7 +51,11 @@ struct Scratch {
     int32_t* qa;
     int32_t* qs;
     int32_t* lvl;
+    uint32_t* bits;  // one bit per vertex: member of the level being pulled from
 };
+
+// Words of the per-worker vertex bitmap.
+__host__ __device__ __forceinline__ size_t bitmap_words(int64_t nv) { return (size_t)(nv + 31) / 32 + 1; }
 
 // Slots of one worker w inside the worker-major scratch arrays.
 struct ScratchBase {
@@ -60,7 +65,8 @@ struct ScratchBase {
     int32_t* qd;
     int32_t* qa;
     int32_t* qs;
-    int32_t* lvl;  // (nv + 2) per worker
+    int32_t* lvl;    // (nv + 2) per worker
+    uint32_t* bits;  // bitmap_words(nv) per worker
     __device__ __forceinline__ Scratch of(int w, int64_t nv) const
     {
         Scratch s;
@@ -72,6 +78,7 @@ struct ScratchBase {
         s.qa = qa + o;
         s.qs = qs + o;
         s.lvl = lvl + (size_t)w * (size_t)(nv + 2);
+        s.bits = bits + (size_t)w * bitmap_words(nv);
         return s;
     }
 };
@@ -85,6 +92,28 @@ __device__ __forceinline__ int vis_deg(const DevGraph& G, int x, int64_t rs, int
     int d = G.deg[x];
     while (d0 < d && G.seq[rs + d0] <= g) ++d0;
     return d0;
+}
+
+// Is y among the first vx (visible) neighbours of x, whose slots start at rx?
+// Binary search of the sorted leading slots, then a scan of the appended tail.
+// Adds the number of slots examined to *cost.
+__device__ __forceinline__ bool has_edge(const DevGraph& G, int x, int64_t rx, int vx, int y, unsigned& cost)
+{
+    const int ns = min(G.nsort[x], vx);
+    int lo = 0, hi = ns;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const int c = G.col[rx + mid];
+        ++cost;
+        if (c < y) lo = mid + 1;
+        else if (c > y) hi = mid;
+        else return true;
+    }
+    for (int s = ns; s < vx; ++s) {
+        ++cost;
+        if (G.col[rx + s] == y) return true;
+    }
+    return false;
 }
 
 __device__ __forceinline__ uint8_t enc_d8(int d)
@@ -228,6 +257,127 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t*
 struct NoPost {
     __device__ void operator()(int, int) const {}
 };
+
+// Edge-balanced walk that sums one value per edge into the edge's source
+// vertex: contrib(j, y, k, dist[k], v) returns whether edge (y,k) contributes
+// and sets v.  Chunking, ILP and gathers are those of lb_walk (never counted as
+// reference traversal).  Instead of one shared atomic per contributing edge,
+// each thread keeps a running sum while its edges share a source vertex and
+// flushes it into s_sum[j] (and ORs kSumHit into s_hit[j], which prep must
+// initialise) only when the source changes; at the end of a chunk a warp whose
+// lanes all hold the same source adds its sums with shuffles first.
+// post(j, y) then sees the chunk's totals.
+// GATHER = false skips the distance gather (contrib then receives 0), for
+// walks whose edge test needs no distance.
+constexpr int kSumHit = 4;
+template <int NT, bool GATHER, class Prep, class Contrib, class Post>
+__device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const int32_t* D, const uint8_t* D8,
+                                            const int32_t* l1, int n1, LbSmem<NT>& sm, double* s_sum, int* s_hit,
+                                            Prep prep, Contrib contrib, Post post)
+{
+    for (int base = 0; base < n1; base += NT) {
+        const int t = threadIdx.x;
+        const int cnt = min(NT, n1 - base);
+        int d = 0;
+        if (t < cnt) {
+            const int x = l1[base + t];
+            const int64_t rs = G.row[x];
+            d = vis_deg(G, x, rs, g);
+            sm.x[t] = x;
+            sm.row[t] = rs;
+            s_sum[t] = 0.0;
+            prep(t, x, d);
+        }
+        int total;
+        const int off = block_exclusive_scan<NT>(d, sm.warp, &total);
+        if (t < cnt) sm.off[t] = off;
+        if (t == 0) {
+            sm.off[cnt] = total;
+            sm.scanned_e += (unsigned)total;
+        }
+        __syncthreads();
+        int j = 0;
+        int cj = -1;       // source vertex of the running sum
+        double cs = 0.0;   // running sum
+        for (int e0 = t; e0 < total; e0 += NT * kEdgeIlp) {
+            int kk[kEdgeIlp], jj[kEdgeIlp], dk[kEdgeIlp];
+#pragma unroll
+            for (int u = 0; u < kEdgeIlp; ++u) {
+                const int e = e0 + u * NT;
+                kk[u] = -1;
+                jj[u] = j;
+                if (e < total) {
+                    if (sm.off[j + 1] <= e) {
+                        int lo = j + 1, hi = cnt - 1;
+                        while (lo < hi) {
+                            int mid = (lo + hi + 1) >> 1;
+                            if (sm.off[mid] <= e) lo = mid;
+                            else hi = mid - 1;
+                        }
+                        j = lo;
+                    }
+                    jj[u] = j;
+                    kk[u] = G.col[sm.row[j] + (e - sm.off[j])];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kEdgeIlp; ++u) dk[u] = (GATHER && kk[u] >= 0) ? (int)D8[kk[u]] : 0;
+            if (GATHER) {
+#pragma unroll
+                for (int u = 0; u < kEdgeIlp; ++u) {
+                    if (dk[u] == SBC_D8_INF) dk[u] = SBC_INF;
+                    else if (dk[u] == SBC_D8_DEEP) dk[u] = D[kk[u]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kEdgeIlp; ++u) {
+                double v;
+                if (kk[u] >= 0 && contrib(jj[u], sm.x[jj[u]], kk[u], dk[u], v)) {
+                    if (jj[u] != cj) {
+                        if (cj >= 0) {
+                            atomicAdd(&s_sum[cj], cs);
+                            atomicOr(&s_hit[cj], kSumHit);
+                        }
+                        cj = jj[u];
+                        cs = 0.0;
+                    }
+                    cs += v;
+                }
+            }
+        }
+        const unsigned full = 0xffffffffu;
+        const int k0 = __shfl_sync(full, cj, 0);
+        if (__all_sync(full, cj == k0) && k0 >= 0) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) cs += __shfl_xor_sync(full, cs, o);
+            if ((t & 31) == 0) {
+                atomicAdd(&s_sum[k0], cs);
+                atomicOr(&s_hit[k0], kSumHit);
+            }
+        } else if (cj >= 0) {
+            atomicAdd(&s_sum[cj], cs);
+            atomicOr(&s_hit[cj], kSumHit);
+        }
+        __syncthreads();
+        if (t < cnt) post(t, sm.x[t]);
+        __syncthreads();
+    }
+}
+
+// Block-wide sum of one double per thread (all threads get the total).
+template <int NT>
+__device__ __forceinline__ double block_sum_f64(double v, double* s_part)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_part[wid] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < NT / 32; ++w) t += s_part[w];
+    __syncthreads();
+    return t;
+}
 
 // Block-wide sum of one 64-bit value per thread (all threads get the total).
 template <int NT>

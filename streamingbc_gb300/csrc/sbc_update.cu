@@ -69,8 +69,13 @@ struct UpdSmem {
     int fl[NT];
     long long part[NT / 32];
     int item, qt, at, st;
-    int root_slot;  // the root's id, as a one-element vertex list
+    int nscan, nprobe;  // level-2 vertices whose parents are found by scan / by probe
 };
+
+// A level-2 vertex looks its parents up by binary search (one probe per root
+// neighbour) instead of scanning its adjacency when its degree exceeds this
+// many times the root's degree; a probe is costed as this many scanned slots.
+constexpr int kProbeRatio = 32;
 
 template <int NT>
 __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, const Scratch& W, int r,
@@ -204,31 +209,32 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
     // cheaper direction is chosen per level by scanned-slot count; results are
     // the same either way.  Used only where no vertex of the level moved (no
     // same-level ex-parent rule applies).
+    // The walked vertices of the level are marked in the worker's bitmap, so a
+    // candidate parent tests a neighbour with one (L2-resident) bit instead of
+    // gathering its distance and state.
     auto pull_walk = [&](const int32_t* plist, int pn) {
-        lb_walk<NT, false>(
-            A.G, g, D, D8, plist, pn, nullptr, 0, sm.lb,
+        lb_walk_sum<NT, false>(
+            A.G, g, D, D8, plist, pn, sm.lb, sm.wn, sm.fl,
             [&](int j, int y, int d) {
                 const int sy = W.st[y];
                 const bool yDown = (sy & SBC_STEP_MASK) != 0;
                 const int64_t oS = S[y];
                 sm.dp[j] = yDown ? ((sy & SBC_MOVED) ? W.dp[y] : oS + W.dp[y]) : oS;
                 sm.wo[j] = (double)oS;
-                sm.wn[j] = 0.0;
                 sm.fl[j] = (yDown ? 1 : 0) | (y == a ? 2 : 0);
             },
-            [&](int j, int y, int c, int dc) {
-                if (dc != L || W.st[c] == 0) return;
+            [&](int j, int y, int c, int, double& v) -> bool {
+                if (!((W.bits[c >> 5] >> (c & 31)) & 1u)) return false;
                 const double wn = W.acc[c];
                 const double wo = __longlong_as_double((long long)W.dp[c]);
-                double v = (double)sm.dp[j] * wn;
+                v = (double)sm.dp[j] * wn;
                 const int fl = sm.fl[j];
                 if (!(fl & 1) && !((fl & 2) && c == b)) v -= sm.wo[j] * wo;
-                atomicAdd(&sm.wn[j], v);
-                if (!(fl & 4)) atomicOr(&sm.fl[j], 4);
+                return true;
             },
             [&](int j, int y) {
                 const int fl = sm.fl[j];
-                if (!(fl & 4)) return;
+                if (!(fl & kSumHit)) return;
                 W.acc[y] += sm.wn[j];  // y's only contributions at this level come from this walk
                 if (!(fl & 1)) {
                     int old = atomicOr(&W.st[y], SBC_ASC);
@@ -240,6 +246,38 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
             });
     };
     long long pull2_cost = -1;  // scanned slots of a level-2 pull (root's neighbours), computed once
+
+    // Level-2 parents of each listed (committed) vertex x: every root
+    // neighbour y (all at level 1) is looked up in x's sorted adjacency; a hit
+    // is a parent, which receives newsigma[y]*wn[x] - [y ascent-only,
+    // (y,x) != (a,b)] sigma[y]*wo[x] and is claimed.  Warp per x, lanes over y.
+    auto probe_parents = [&](const int32_t* list, int n, int64_t rrow, int rdeg) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        unsigned cost = 0;
+        for (int i = warp; i < n; i += NT / 32) {
+            const int x = list[i];
+            const int64_t rx = A.G.row[x];
+            const int vx = vis_deg(A.G, x, rx, g);
+            const double wn = W.acc[x];
+            const double wo = __longlong_as_double((long long)W.dp[x]);
+            for (int t = lane; t < rdeg; t += 32) {
+                const int y = A.G.col[rrow + t];
+                if (!has_edge(A.G, x, rx, vx, y, cost)) continue;
+                const int sy = W.st[y];
+                const bool yDown = (sy & SBC_STEP_MASK) != 0;
+                if (!yDown && !(sy & SBC_ASC)) {
+                    int old = atomicOr(&W.st[y], SBC_ASC);
+                    if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = y;
+                }
+                const int64_t nSy = yDown ? ((sy & SBC_MOVED) ? W.dp[y] : S[y] + W.dp[y]) : S[y];
+                double v = (double)nSy * wn;
+                if (!yDown && !(y == a && x == b)) v -= (double)S[y] * wo;
+                atomicAdd(&W.acc[y], v);
+            }
+        }
+        atomicAdd(&sm.lb.scanned_e, (unsigned long long)cost);
+        __syncthreads();
+    };
 
     int ua_lo = 0, ua_hi = 0;
     const int Lmax = Lb + nsteps - 1;
@@ -253,28 +291,73 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         }
         const int next_lo = sm.at;
         const bool pull_ok = L >= 1 && L <= 2 && (!moving || L < Lb);
-        if (pull_ok) {
-            // Commit every vertex of the level; keep its push weights in acc/dp;
-            // count it as traversed (reference counters) and sum its degree.
+        if (pull_ok || L == 0) {
+            // Commit every vertex x of the level and keep its push weights in
+            // its acc/dp slots; count it as traversed (reference counters).
+            //   L == 0  the root alone: no parents, committing is all.
+            //   L == 1  the only parent is the root (sigma 1): each x's
+            //           contribution is summed straight into the root, no scan.
+            //   L == 2  parents are N(x) ∩ N(root).  Per vertex, either scan
+            //           N(x) for distance-1 neighbours (push), or, when N(x) is
+            //           much longer than N(root), look each root neighbour up
+            //           in x's sorted adjacency (probe); or, for the whole
+            //           level, let the root's neighbours pull (bitmap test).
+            //           The cheapest plan by scanned slots is taken.
             const int na_ = ua_hi - ua_lo;
-            long long push_cost = 0;
+            const int64_t rrow = A.G.row[root];
+            const int rdeg = vis_deg(A.G, root, rrow, g);
+            const int rs = W.st[root];
+            const bool rootDown = (rs & SBC_STEP_MASK) != 0;
+            const double rS = (double)S[root];
+            const double rnS = rootDown ? (double)((rs & SBC_MOVED) ? W.dp[root] : S[root] + W.dp[root]) : rS;
+            if (threadIdx.x == 0) {
+                sm.nscan = 0;
+                sm.nprobe = 0;
+            }
+            __syncthreads();
+            long long push_cost = 0, mixed_cost = 0;
+            double root_sum = 0.0;
+            const int qbase = sm.st;  // free tail of the same-level queue holds the two lists
             for (int i = threadIdx.x; i < dn + na_; i += NT) {
                 const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
                 double wn, wo;
                 commit(x, wn, wo);
                 W.acc[x] = wn;
                 W.dp[x] = (int64_t)__double_as_longlong(wo);
-                push_cost += vis_deg(A.G, x, A.G.row[x], g);
+                const int dx = vis_deg(A.G, x, A.G.row[x], g);
+                push_cost += dx;
+                if (L == 1) {
+                    double v = rnS * wn;
+                    if (!rootDown && !(root == a && x == b)) v -= rS * wo;
+                    root_sum += v;
+                } else if (L == 2) {
+                    atomicOr(&W.bits[x >> 5], 1u << (x & 31));
+                    if ((long long)dx > (long long)kProbeRatio * rdeg) {
+                        W.qs[nv - 1 - atomicAdd(&sm.nprobe, 1)] = x;
+                        mixed_cost += (long long)kProbeRatio * rdeg;
+                    } else {
+                        W.qs[qbase + atomicAdd(&sm.nscan, 1)] = x;
+                        mixed_cost += dx;
+                    }
+                }
             }
             push_cost = block_sum<NT>(push_cost, sm.part);
-            long long pull_cost = 0;
-            const int64_t rrow = A.G.row[root];
-            const int rdeg = vis_deg(A.G, root, rrow, g);
-            if (dn + na_ == 0) {
-                pull_cost = 1;  // nothing to walk at this level; the (empty) push walk is a no-op
-            } else if (L == 1) {
-                pull_cost = rdeg;
-            } else {
+            if (threadIdx.x == 0) {
+                sm.lb.walked_v += (unsigned)(dn + na_);
+                sm.lb.walked_e += (unsigned long long)push_cost;
+            }
+            if (L == 1) {
+                root_sum = block_sum_f64<NT>(root_sum, (double*)sm.part);
+                if (threadIdx.x == 0 && dn + na_ > 0) {
+                    W.acc[root] += root_sum;
+                    if (!rootDown) {
+                        int old = atomicOr(&W.st[root], SBC_ASC);
+                        if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = root;
+                    }
+                }
+                __syncthreads();
+            } else if (L == 2 && dn + na_ > 0) {
+                mixed_cost = block_sum<NT>(mixed_cost, sm.part);
                 if (pull2_cost < 0) {
                     long long c = 0;
                     for (int i = threadIdx.x; i < rdeg; i += NT) {
@@ -283,20 +366,19 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
                     }
                     pull2_cost = block_sum<NT>(c, sm.part);
                 }
-                pull_cost = pull2_cost;
-            }
-            if (threadIdx.x == 0) {
-                sm.lb.walked_v += (unsigned)(dn + na_);
-                sm.lb.walked_e += (unsigned long long)push_cost;
-                sm.root_slot = root;
-            }
-            __syncthreads();
-            if (pull_cost < push_cost) {
-                if (L == 1) pull_walk(&sm.root_slot, 1);
-                else pull_walk(A.G.col + rrow, rdeg);
-            } else {
-                lb_walk<NT, false>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, na_, sm.lb, prep_loaded,
-                                   [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+                if (pull2_cost < mixed_cost) {
+                    pull_walk(A.G.col + rrow, rdeg);
+                } else {
+                    const int nscan = sm.nscan, nprobe = sm.nprobe;
+                    lb_walk<NT, false>(A.G, g, D, D8, W.qs + qbase, nscan, nullptr, 0, sm.lb, prep_loaded,
+                                       [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+                    probe_parents(W.qs + nv - nprobe, nprobe, rrow, rdeg);
+                }
+                for (int i = threadIdx.x; i < dn + na_; i += NT) {
+                    const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
+                    W.bits[x >> 5] = 0u;  // words hold only this level's marks
+                }
+                __syncthreads();
             }
         } else if (!moving) {
             lb_walk<NT>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,

@@ -112,6 +112,43 @@ def test_deep_levels_use_exact_fallback(sbc_lib, port_lib):
         check_state(f, o.level(), o.sigma(), o.bc())
 
 
+def test_hub_parents_direct_probe_scan_and_pull(sbc_lib, port_lib):
+    """Roots of degree 1-2 above hubs: level-1 contributions go straight to the
+    root, level-2 hubs find their parents by binary search in their sorted
+    adjacency (and through the unsorted tail that insertions append), smaller
+    level-2 vertices scan, and other roots pull.  State checked against the
+    oracle after every insertion."""
+    rng = np.random.default_rng(17)
+    n = 3000
+    us, vs = [0, 0], [1, 2]
+    for h in (1, 2):                       # two hubs under root 0
+        nb = rng.choice(np.arange(3, 1500), size=700, replace=False)
+        us += [h] * nb.size
+        vs += nb.tolist()
+    nb = rng.choice(np.arange(1500, n), size=1200, replace=False)
+    us += [3] * nb.size                    # a level-2 hub with a level-3 fan
+    vs += nb.tolist()
+    extra = rng.integers(3, n, size=(1500, 2))
+    us += extra[:, 0].tolist()
+    vs += extra[:, 1].tolist()
+    g = G.from_edges(n, np.array(us), np.array(vs))
+    roots = np.array([0, 4, 1601, 2999, 1, 3], dtype=np.int64)
+    ins = [(1, 2999), (3, 1), (2, 1700), (0, 5), (1, 1800), (1, 1801), (3, 4), (2, 2500), (10, 11), (1, 1999)]
+    ins = np.array([p for p in ins if p[1] not in set(g.adj[g.off[p[0]]:g.off[p[0] + 1]].tolist())], dtype=np.int64)
+    ins = np.concatenate([ins, G.uniform_insertions(g, 30, seed=5)])
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots, nthreads=2)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    check_state(f, o.level(), o.sigma(), o.bc())
+    for u, v in ins:
+        o.insert(int(u), int(v))
+        st = f.insert([(u, v)])
+        c = o.counters()
+        assert (st["vertices"], st["edges"]) == (c["vertices"], c["edges"])
+        check_state(f, o.level(), o.sigma(), o.bc())
+
+
 @pytest.mark.parametrize("workers", [1, 3])
 def test_few_workers_same_result(sbc_lib, workers):
     z = load_golden("rmat9")
