@@ -166,6 +166,47 @@ int sbc_reset_profile(sbc_forest *f);
 int sbc_timer_start(sbc_forest *f);
 int sbc_timer_stop(sbc_forest *f, double *ms);
 
+/* ---- static init that allocates nothing ---------------------------------- */
+
+/* This entry point has no counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc themselves or let a library do it
+ * -- code running inside another runtime that owns the device memory pool,
+ * or a process whose device memory is reserved up front -- this runs the
+ * static Brandes init (the same kernel as sbc_static_init) with all of its
+ * scratch taken from one fixed array compiled into libsbc_gb300.so: every GPU
+ * that loads the library holds SBC_NOALLOC_SCRATCH_BYTES (about 37 MiB) of
+ * device memory for it until the process exits.  The call allocates nothing:
+ * no cudaMalloc, no cudaFree, no allocating library routine.
+ *
+ * All pointers are DEVICE memory owned by the caller:
+ *   d_off[nv+1] int64, d_col[d_off[nv]] int32  symmetric CSR of the graph
+ *   d_roots[nk] int64                          distinct root vertices
+ *   d_dist[nk][nv] int32 (INT32_MAX = unreachable), d_sigma[nk][nv] int64,
+ *   d_delta[nk][nv] fp64, d_bc[nv] fp64         outputs, as sbc_get_dist/...
+ * Limits: nv <= SBC_NOALLOC_MAX_VERTICES and nk * nv <= SBC_NOALLOC_MAX_CELLS;
+ * larger sizes are rejected with SBC_ERR_ARG before any GPU work.
+ * The work is queued on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream) and the call returns without waiting.
+ *
+ * The first call on a device looks up the device address of the array on the
+ * current device (cudaGetSymbolAddress); make that first call before any CUDA
+ * stream capture.  Every call on a device uses the same array and leaves its
+ * contents behind for the next; what must start at zero is cleared on the
+ * stream at the start of each call.  Calls whose GPU work overlaps -- on
+ * different streams, or from different host threads -- race on the array and
+ * give undefined results: serialise them.
+ * Errors: SBC_ERR_ARG, SBC_ERR_NOGPU, SBC_ERR_CUDA; message from
+ * sbc_noalloc_last_error(). */
+#define SBC_NOALLOC_MAX_VERTICES 262144
+#define SBC_NOALLOC_MAX_CELLS 4194304
+#define SBC_NOALLOC_WORKERS 8
+#define SBC_NOALLOC_SCRATCH_BYTES 38797824
+int sbc_static_init_noalloc(int64_t nv, const int64_t *d_off, const int32_t *d_col, int64_t nk,
+                            const int64_t *d_roots, int32_t *d_dist, int64_t *d_sigma, double *d_delta,
+                            double *d_bc, void *stream);
+const char *sbc_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,9 @@
 // BC is then a column sum of delta over roots excluding each root itself
 // (init.c:175-177), computed by k_bc_colsum in root order.
 #include <climits>
+#include <mutex>
+#include <string>
+#include "sbc_gb300.h"
 #include "sbc_host.h"
 #include "sbc_internal.cuh"
 
@@ -185,3 +188,132 @@ cudaError_t launch_static(sbc_forest* f)
 }
 
 }  // namespace sbc
+
+// ===========================================================================
+// Static init without any allocation by the library.
+//
+// For callers that cannot call cudaMalloc -- code running inside another
+// runtime's memory pool, or a host process whose device memory is fully
+// reserved up front -- sbc_static_init_noalloc runs the same k_static kernel
+// with every byte of its scratch (per-worker queues, level offsets and
+// accumulators, the one-byte distance rows, the CSR degrees and the counters)
+// carved out of one file-scope device array, g_noalloc_scratch, below.  The
+// caller passes the graph and the outputs in its own device memory.  Every GPU
+// that loads the library holds this array until the process exits.
+// ===========================================================================
+
+namespace sbc {
+namespace {
+
+constexpr int64_t kNoallocMaxVertices = SBC_NOALLOC_MAX_VERTICES;
+constexpr int64_t kNoallocMaxCells = SBC_NOALLOC_MAX_CELLS;  // roots x vertices
+constexpr int kNoallocSlots = SBC_NOALLOC_WORKERS;
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+// Layout of the array (byte offsets; each region 256-byte aligned).
+constexpr size_t kOffCounters = 0;  // work counter + traversal counters
+constexpr size_t kOffDeg = align256(kOffCounters + 16 * sizeof(unsigned long long));
+constexpr size_t kOffQd = align256(kOffDeg + sizeof(int32_t) * kNoallocMaxVertices);
+constexpr size_t kOffLvl = align256(kOffQd + sizeof(int32_t) * kNoallocSlots * kNoallocMaxVertices);
+constexpr size_t kOffAcc = align256(kOffLvl + sizeof(int32_t) * kNoallocSlots * (kNoallocMaxVertices + 2));
+constexpr size_t kOffDist8 = align256(kOffAcc + sizeof(double) * kNoallocSlots * kNoallocMaxVertices);
+constexpr size_t kNoallocBytes = align256(kOffDist8 + kNoallocMaxCells);
+static_assert(kNoallocBytes == SBC_NOALLOC_SCRATCH_BYTES, "scratch size in sbc_gb300.h is out of date");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+// Device address of g_noalloc_scratch, looked up once per device.
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[256] = {};
+
+__global__ void k_csr_degrees(const int64_t* __restrict__ off, int64_t nv, int32_t* __restrict__ deg)
+{
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x)
+        deg[v] = (int32_t)(off[v + 1] - off[v]);
+}
+
+thread_local std::string t_noalloc_err;
+
+int noalloc_fail(int code, const char* msg)
+{
+    t_noalloc_err = msg;
+    return code;
+}
+
+}  // namespace
+
+}  // namespace sbc
+
+extern "C" const char* sbc_noalloc_last_error(void) { return sbc::t_noalloc_err.c_str(); }
+
+extern "C" int sbc_static_init_noalloc(int64_t nv, const int64_t* d_off, const int32_t* d_col, int64_t nk,
+                                       const int64_t* d_roots, int32_t* d_dist, int64_t* d_sigma, double* d_delta,
+                                       double* d_bc, void* stream)
+{
+    using namespace sbc;
+    if (nv < 1 || nk < 1 || !d_off || !d_col || !d_roots || !d_dist || !d_sigma || !d_delta || !d_bc)
+        return noalloc_fail(SBC_ERR_ARG, "sbc_static_init_noalloc: null pointer or empty graph/root set");
+    if (nv > kNoallocMaxVertices)
+        return noalloc_fail(SBC_ERR_ARG, "sbc_static_init_noalloc: more vertices than SBC_NOALLOC_MAX_VERTICES");
+    if (nk > nv || nk * nv > kNoallocMaxCells)
+        return noalloc_fail(SBC_ERR_ARG,
+                            "sbc_static_init_noalloc: roots x vertices exceeds SBC_NOALLOC_MAX_CELLS (or nk > nv)");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256)
+        return noalloc_fail(SBC_ERR_NOGPU, "sbc_static_init_noalloc: no current CUDA device");
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+                return noalloc_fail(SBC_ERR_CUDA, "sbc_static_init_noalloc: cudaGetSymbolAddress failed");
+            g_noalloc_ptr[dev] = p;
+        }
+        base = (unsigned char*)g_noalloc_ptr[dev];
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long* counters = (unsigned long long*)(base + kOffCounters);
+    int32_t* deg = (int32_t*)(base + kOffDeg);
+    const int slots = (int)std::min<int64_t>(kNoallocSlots, nk);
+    // Clear what must start at zero: the work and traversal counters and the
+    // accumulators (a previous call leaves them zero, but a call that failed
+    // half-way may not have).
+    if (cudaMemsetAsync(counters, 0, 16 * sizeof(unsigned long long), s) != cudaSuccess ||
+        cudaMemsetAsync(base + kOffAcc, 0, sizeof(double) * (size_t)slots * (size_t)nv, s) != cudaSuccess)
+        return noalloc_fail(SBC_ERR_CUDA, "sbc_static_init_noalloc: clearing scratch failed");
+    const int dgrid = (int)std::min<int64_t>((nv + 255) / 256, 4096);
+    k_csr_degrees<<<dgrid, 256, 0, s>>>(d_off, nv, deg);
+
+    StaticArgs A;
+    A.G.nv = nv;
+    A.G.row = d_off;
+    A.G.deg = deg;   // plain CSR: every slot is visible (deg0 == deg)
+    A.G.deg0 = deg;
+    A.G.nsort = deg;
+    A.G.col = d_col;
+    A.G.seq = d_col;  // never read when deg0 == deg
+    A.nv = nv;
+    A.nk = (int)nk;
+    A.roots = d_roots;
+    A.dist = d_dist;
+    A.dist8 = base + kOffDist8;
+    A.sigma = d_sigma;
+    A.delta = d_delta;
+    // k_static uses only the queue, level-offset and accumulator slots; the
+    // others point at valid (unused) memory.
+    A.scr.st = (int32_t*)(base + kOffQd);
+    A.scr.dp = (int64_t*)(base + kOffAcc);
+    A.scr.qa = (int32_t*)(base + kOffQd);
+    A.scr.qs = (int32_t*)(base + kOffQd);
+    A.scr.bits = (uint32_t*)(base + kOffQd);
+    A.scr.qd = (int32_t*)(base + kOffQd);
+    A.scr.lvl = (int32_t*)(base + kOffLvl);
+    A.scr.acc = (double*)(base + kOffAcc);
+    A.work_counter = (int*)(counters + 8);
+    A.counters = counters;
+    k_static<1024><<<slots, 1024, 0, s>>>(A);
+    k_bc_colsum<<<dgrid, 256, 0, s>>>(d_delta, d_roots, (int)nk, nv, d_bc);
+    if (cudaGetLastError() != cudaSuccess) return noalloc_fail(SBC_ERR_CUDA, "sbc_static_init_noalloc: launch failed");
+    return SBC_OK;
+}
