@@ -378,6 +378,7 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_update", "alg_bytes_per_launch": alg_bytes / upd_launches,
                          "alg_bytes_ref_per_launch": alg_bytes_ref / upd_launches,
+                         "frac_ref_equivalent": (alg_bytes_ref / upd_launches) / (upd_ms / 1e3) / 1e9 / peak,
                          "avg_launch_ms": upd_ms},
             "cpu_baseline": cpu,
             "e2e": e2e,
