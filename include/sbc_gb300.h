@@ -133,6 +133,13 @@ int sbc_insert_batch(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *
  * that finds no slack is not applied and the next sbc_sync reports it. */
 int sbc_insert_batch_device(sbc_forest *f, int64_t n, const int32_t *d_u, const int32_t *d_v);
 
+/* Replay device-input batches from CUDA graphs (on by default): each batch
+ * size is captured once (input copies, append, classify, update, seal) and
+ * replayed with only the input copies re-pointed; re-captured after an
+ * adjacency re-pack.  Not used while profiling is on.  Results are the same
+ * either way. */
+int sbc_set_graph_capture(sbc_forest *f, int on);
+
 /* Apply n insertions whose edges are ALREADY in the adjacency (inserted by
  * sbc_graph_insert_directed in both directions), exactly like
  * insertEdgeStreamingBC after the caller's stinger_insert_edge calls.

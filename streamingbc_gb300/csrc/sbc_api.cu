@@ -210,6 +210,62 @@ int collect_stats(sbc_forest* f, int64_t n, sbc_batch_stats* st)
     return SBC_OK;
 }
 
+// One device-input batch: the endpoints' addresses are recorded on the stream
+// (k_set_src), then staging, append, classify, update and seal run from a CUDA
+// graph captured once per batch size n and replayed unchanged.  Falls back to
+// direct launches (and stops capturing) if the capture is refused.
+int launch_batch_direct(sbc_forest* f, int n)
+{
+    sbc_graph* g = f->g;
+    CK(sbc::launch_stage(g, n));
+    CK(sbc::launch_append(g, n, false));
+    CK(sbc::launch_update(f, n, false));
+    CK(sbc::launch_seal(g, n));
+    return SBC_OK;
+}
+
+int replay_batch(sbc_forest* f, int n, const int32_t* d_u, const int32_t* d_v)
+{
+    sbc_graph* g = f->g;
+    CK(sbc::launch_set_src(g, d_u, d_v));
+    sbc_forest::CapturedBatch* cb = nullptr;
+    for (auto& p : f->captured)
+        if (p.first == n) cb = &p.second;
+    if (cb && cb->exec && (cb->repacks != g->repacks || cb->d_ins != g->d_ins)) {
+        cudaGraphExecDestroy(cb->exec);
+        cb->exec = nullptr;
+    }
+    if (!cb || !cb->exec) {
+        if (!cb) {
+            f->captured.emplace_back(n, sbc_forest::CapturedBatch());
+            cb = &f->captured.back().second;
+        }
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal);
+        if (!e) {
+            cudaError_t el = sbc::launch_stage(g, n);
+            if (!el) el = sbc::launch_append(g, n, false);
+            if (!el) el = sbc::launch_update(f, n, false);
+            if (!el) el = sbc::launch_seal(g, n);
+            e = cudaStreamEndCapture(g->stream, &graph);
+            if (!e) e = el;
+        }
+        if (!e) e = cudaGraphInstantiate(&cb->exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e) {
+            cudaGetLastError();
+            if (cb->exec) cudaGraphExecDestroy(cb->exec);
+            cb->exec = nullptr;
+            f->use_graphs = false;  // capture refused here: launch directly from now on
+            return launch_batch_direct(f, n);
+        }
+        cb->repacks = g->repacks;
+        cb->d_ins = g->d_ins;
+    }
+    CK(cudaGraphLaunch(cb->exec, g->stream));
+    return SBC_OK;
+}
+
 int check_graph_err(sbc_graph* g)
 {
     int err = 0;
@@ -225,6 +281,7 @@ int check_graph_err(sbc_graph* g)
 template <class T>
 int get_rows(sbc_forest* f, const T* base, int64_t r0, int64_t nr, T* out)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "state read: the forest's graph was destroyed");
     if (!f || !out || r0 < 0 || nr < 0 || r0 + nr > f->nk) return fail(SBC_ERR_ARG, "state read: bad row range");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(cudaMemcpyAsync(out, base + (size_t)r0 * f->nv, sizeof(T) * (size_t)nr * f->nv, cudaMemcpyDeviceToHost,
@@ -298,7 +355,8 @@ int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int6
     if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) || (e = dev_alloc(&g->d_row, nv + 1)) ||
         (e = dev_alloc(&g->d_deg, nv)) || (e = dev_alloc(&g->d_deg0, nv)) || (e = dev_alloc(&g->d_cap, nv)) ||
         (e = dev_alloc(&g->d_nsort, nv)) ||
-        (e = dev_alloc(&g->d_col, total)) || (e = dev_alloc(&g->d_seq, total)) || (e = dev_alloc(&g->d_err, 1))) {
+        (e = dev_alloc(&g->d_col, total)) || (e = dev_alloc(&g->d_seq, total)) || (e = dev_alloc(&g->d_err, 1)) ||
+        (e = dev_alloc(&g->d_src, 2))) {
         sbc_graph_destroy(g);
         return cuda_fail(e, "sbc_graph_create allocation");
     }
@@ -326,6 +384,7 @@ int sbc_graph_destroy(sbc_graph* g)
     if (!g) return SBC_OK;
     use_device(g->device);
     if (g->stream) cudaStreamSynchronize(g->stream);
+    for (sbc_forest* f : g->forests) f->g = nullptr;  // forests outliving their graph are detached
     dev_free(g->d_row);
     dev_free(g->d_deg);
     dev_free(g->d_deg0);
@@ -334,6 +393,7 @@ int sbc_graph_destroy(sbc_graph* g)
     dev_free(g->d_col);
     dev_free(g->d_seq);
     dev_free(g->d_err);
+    dev_free(g->d_src);
     dev_free(g->d_ins);
     if (g->h_ins) cudaFreeHost(g->h_ins);
     if (g->stream) cudaStreamDestroy(g->stream);
@@ -454,6 +514,7 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     if (use_device(g->device)) return SBC_ERR_CUDA;
     sbc_forest* f = new sbc_forest();
     f->g = g;
+    f->device = g->device;
     f->nv = g->nv;
     f->nk = nk;
     f->variant = variant;
@@ -507,6 +568,7 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     CK(cudaEventCreate(&f->t0));
     CK(cudaEventCreate(&f->t1));
     CK(cudaStreamSynchronize(g->stream));
+    g->forests.push_back(f);
     *out = f;
     return SBC_OK;
 }
@@ -514,9 +576,11 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
 int sbc_forest_destroy(sbc_forest* f)
 {
     if (!f) return SBC_OK;
+    use_device(f->device);
     if (f->g) {
-        use_device(f->g->device);
         cudaStreamSynchronize(f->g->stream);
+        auto& fs = f->g->forests;
+        fs.erase(std::remove(fs.begin(), fs.end(), f), fs.end());
     }
     dev_free(f->d_roots);
     dev_free(f->d_dist);
@@ -536,6 +600,8 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_lvl);
     dev_free(f->d_bits);
     f->prof_release();
+    for (auto& p : f->captured)
+        if (p.second.exec) cudaGraphExecDestroy(p.second.exec);
     if (f->t0) cudaEventDestroy(f->t0);
     if (f->t1) cudaEventDestroy(f->t1);
     delete f;
@@ -554,6 +620,7 @@ int sbc_forest_info(const sbc_forest* f, int64_t* nv, int64_t* nk, int64_t* work
 
 int sbc_static_init(sbc_forest* f)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_static_init: the forest's graph was destroyed");
     if (!f) return fail(SBC_ERR_ARG, "sbc_static_init: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(sbc::launch_static(f));
@@ -563,6 +630,7 @@ int sbc_static_init(sbc_forest* f)
 
 int sbc_insert_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, sbc_batch_stats* stats)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_insert_batch: the forest's graph was destroyed");
     if (!f || n < 0 || (n > 0 && (!u || !v))) return fail(SBC_ERR_ARG, "sbc_insert_batch: bad arguments");
     if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_insert_batch before sbc_static_init");
     if (n >= INT32_MAX) return fail(SBC_ERR_ARG, "batch too large");
@@ -590,6 +658,7 @@ int sbc_insert_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* 
 
 int sbc_insert_batch_device(sbc_forest* f, int64_t n, const int32_t* d_u, const int32_t* d_v)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_insert_batch_device: the forest's graph was destroyed");
     if (!f || n < 0 || (n > 0 && (!d_u || !d_v))) return fail(SBC_ERR_ARG, "sbc_insert_batch_device: bad arguments");
     if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_insert_batch_device before sbc_static_init");
     if (n >= INT32_MAX) return fail(SBC_ERR_ARG, "batch too large");
@@ -598,10 +667,10 @@ int sbc_insert_batch_device(sbc_forest* f, int64_t n, const int32_t* d_u, const 
     if (use_device(g->device)) return SBC_ERR_CUDA;
     int rc = ensure_staging(g, n);
     if (rc) return rc;
-    const int cap = g->ins_capacity;
+    if (f->use_graphs && !f->prof) return replay_batch(f, (int)n, d_u, d_v);
     f->prof_begin(sbc::PROF_BATCH);
-    CK(cudaMemcpyAsync(g->d_ins, d_u, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, g->stream));
-    CK(cudaMemcpyAsync(g->d_ins + cap, d_v, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, g->stream));
+    CK(sbc::launch_set_src(g, d_u, d_v));
+    CK(sbc::launch_stage(g, (int)n));
     f->prof_begin(sbc::PROF_APPEND);
     CK(sbc::launch_append(g, (int)n, false));
     f->prof_end(sbc::PROF_APPEND);
@@ -611,8 +680,16 @@ int sbc_insert_batch_device(sbc_forest* f, int64_t n, const int32_t* d_u, const 
     return SBC_OK;
 }
 
+int sbc_set_graph_capture(sbc_forest* f, int on)
+{
+    if (!f) return fail(SBC_ERR_ARG, "sbc_set_graph_capture: null");
+    f->use_graphs = on != 0;
+    return SBC_OK;
+}
+
 int sbc_update_inserted(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, sbc_batch_stats* stats)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_update_inserted: the forest's graph was destroyed");
     if (!f || n < 0 || (n > 0 && (!u || !v))) return fail(SBC_ERR_ARG, "sbc_update_inserted: bad arguments");
     if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_update_inserted before sbc_static_init");
     sbc_graph* g = f->g;
@@ -634,6 +711,7 @@ int sbc_update_inserted(sbc_forest* f, int64_t n, const int64_t* u, const int64_
 
 int sbc_sync(sbc_forest* f)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_sync: the forest's graph was destroyed");
     if (!f) return fail(SBC_ERR_ARG, "sbc_sync: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(cudaStreamSynchronize(f->g->stream));
@@ -643,6 +721,7 @@ int sbc_sync(sbc_forest* f)
 int sbc_read_counters(sbc_forest* f, int64_t* vertices, int64_t* edges, int64_t* case1, int64_t* case2,
                       int64_t* scanned)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_read_counters: the forest's graph was destroyed");
     if (!f) return fail(SBC_ERR_ARG, "sbc_read_counters: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     unsigned long long c[SBC_NCOUNTERS];
@@ -659,6 +738,7 @@ int sbc_read_counters(sbc_forest* f, int64_t* vertices, int64_t* edges, int64_t*
 
 int sbc_get_bc(sbc_forest* f, double* out)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_get_bc: the forest's graph was destroyed");
     if (!f || !out) return fail(SBC_ERR_ARG, "sbc_get_bc: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(cudaMemcpyAsync(out, f->d_bc, sizeof(double) * f->nv, cudaMemcpyDeviceToHost, f->g->stream));
@@ -679,6 +759,7 @@ int sbc_set_profiling(sbc_forest* f, int on)
 
 int sbc_get_profile(sbc_forest* f, sbc_profile* out)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_get_profile: the forest's graph was destroyed");
     if (!f || !out) return fail(SBC_ERR_ARG, "sbc_get_profile: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     for (int k = 0; k < sbc::PROF_COUNT; ++k) f->prof_collect(k);
@@ -708,6 +789,7 @@ int sbc_reset_profile(sbc_forest* f)
 
 int sbc_timer_start(sbc_forest* f)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_timer_start: the forest's graph was destroyed");
     if (!f) return fail(SBC_ERR_ARG, "sbc_timer_start: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(cudaEventRecord(f->t0, f->g->stream));
@@ -716,6 +798,7 @@ int sbc_timer_start(sbc_forest* f)
 
 int sbc_timer_stop(sbc_forest* f, double* ms)
 {
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_timer_stop: the forest's graph was destroyed");
     if (!f || !ms) return fail(SBC_ERR_ARG, "sbc_timer_stop: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(cudaEventRecord(f->t1, f->g->stream));

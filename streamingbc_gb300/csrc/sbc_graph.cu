@@ -59,6 +59,41 @@ __global__ void k_append(int64_t nv, const int64_t* __restrict__ row, int32_t* d
     }
 }
 
+// A batch's endpoint arrays live in the caller's device memory.  k_set_src
+// records their addresses in the graph's two-pointer slot (its arguments are
+// copied at launch, so nothing on the host has to outlive the call), and
+// k_stage_inputs, which a captured batch graph replays unchanged, copies from
+// the addresses in the slot into the staging rows (u at dst[0..n), v at
+// dst[cap..cap+n)).
+__global__ void k_set_src(const int32_t** slot, const int32_t* u, const int32_t* v)
+{
+    slot[0] = u;
+    slot[1] = v;
+}
+
+__global__ void k_stage_inputs(const int32_t* const* __restrict__ slot, int32_t* dst, int cap, int n)
+{
+    const int32_t* u = slot[0];
+    const int32_t* v = slot[1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        dst[i] = u[i];
+        dst[cap + i] = v[i];
+    }
+}
+
+cudaError_t launch_set_src(sbc_graph* g, const int32_t* d_u, const int32_t* d_v)
+{
+    k_set_src<<<1, 1, 0, g->stream>>>(g->d_src, d_u, d_v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stage(sbc_graph* g, int n)
+{
+    const int blocks = std::min((n + 255) / 256, 1024);
+    k_stage_inputs<<<blocks < 1 ? 1 : blocks, 256, 0, g->stream>>>(g->d_src, g->d_ins, g->ins_capacity, n);
+    return cudaGetLastError();
+}
+
 // After a batch: every appended slot becomes visible to all later traversals.
 __global__ void k_seal(int n, const int32_t* __restrict__ iu, const int32_t* __restrict__ iv,
                        const int32_t* __restrict__ ok, const int32_t* __restrict__ deg, int32_t* deg0)

@@ -14,6 +14,8 @@ enum ProfKernel { PROF_STATIC = 0, PROF_APPEND, PROF_CLASSIFY, PROF_UPDATE, PROF
 
 }  // namespace sbc
 
+struct sbc_forest;
+
 // Device-resident slack-CSR adjacency (replaces the STINGER edge-block store,
 // src/stinger/stinger-internal.h:45-103).  All device work for the graph and
 // for forests bound to it runs on `stream`, in order.
@@ -38,7 +40,10 @@ struct sbc_graph {
     int ins_capacity = 0;
     int32_t* d_ins = nullptr;  // [3 * ins_capacity]: u, v, ok
     int32_t* h_ins = nullptr;  // pinned [2 * ins_capacity]
+    const int32_t** d_src = nullptr;  // device slot: addresses of the caller's endpoint arrays
     int64_t repacks = 0;
+    // forests bound to this graph; destroying the graph detaches them
+    std::vector<sbc_forest*> forests;
 
     sbc::DevGraph dev() const
     {
@@ -55,7 +60,8 @@ struct sbc_graph {
 };
 
 struct sbc_forest {
-    sbc_graph* g = nullptr;
+    sbc_graph* g = nullptr;  // null once the graph has been destroyed
+    int device = 0;
     int64_t nv = 0, nk = 0;
     std::vector<int64_t> h_roots;
     int64_t* d_roots = nullptr;
@@ -84,6 +90,16 @@ struct sbc_forest {
     // case-1 pairs, case-2 pairs, adjacency slots actually scanned
     unsigned long long* d_counters = nullptr;
     int64_t bytes = 0;
+    // Device-input batches replayed from captured CUDA graphs, one per batch
+    // size; only the two input copies are re-pointed per call.  A graph is
+    // re-captured when the adjacency was re-packed or the staging moved.
+    struct CapturedBatch {
+        cudaGraphExec_t exec = nullptr;
+        int64_t repacks = -1;
+        const int32_t* d_ins = nullptr;
+    };
+    bool use_graphs = true;
+    std::vector<std::pair<int, CapturedBatch>> captured;
     // profiling: a ring of CUDA event pairs per kernel kind; pairs are read
     // back only when the ring wraps or the profile is queried, so recording
     // never makes the host wait for the device.
@@ -176,6 +192,10 @@ cudaError_t launch_static(sbc_forest* f);
 // (u, v, ok rows).  `all_visible` ignores the per-slot sequence numbers.
 cudaError_t launch_update(sbc_forest* f, int n, bool all_visible);
 cudaError_t launch_append(sbc_graph* g, int n, bool directed);
+// Record the addresses of device-resident endpoint arrays (one-thread kernel),
+// then copy them into the staging rows (the part a batch graph replays).
+cudaError_t launch_set_src(sbc_graph* g, const int32_t* d_u, const int32_t* d_v);
+cudaError_t launch_stage(sbc_graph* g, int n);
 cudaError_t launch_seal(sbc_graph* g, int n);
 cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq);
 }  // namespace sbc

@@ -364,33 +364,87 @@ __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const int3
     }
 }
 
-// Block-wide sum of one double per thread (all threads get the total).
+// Block-wide sums of two 64-bit integers and one double per thread; every
+// thread gets the three totals.  Warps reduce with shuffles, then warp 0 adds
+// the per-warp partials and publishes the totals.  GB300 issues fp64 at a
+// small fraction of its fp32 rate (every warp-wide fp64 instruction holds the
+// SM's fp64 pipe for many cycles), so the double is shuffled only in warps
+// where some lane holds a nonzero value, and the tail is one warp's work
+// rather than every thread adding all partials.  s_part holds 3 * (NT/32) + 3
+// entries.
 template <int NT>
-__device__ __forceinline__ double block_sum_f64(double v, double* s_part)
+__device__ __forceinline__ void block_sum3(long long& a, long long& b, double& c, long long* s_part)
 {
+    constexpr int NW = NT / 32;
+    static_assert(NW <= 32, "one warp adds the partials");
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) s_part[wid] = v;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(full, a, o);
+        b += __shfl_xor_sync(full, b, o);
+    }
+    if (__any_sync(full, __double_as_longlong(c) != 0)) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(full, c, o);
+    }
+    if (lane == 0) {
+        s_part[3 * wid] = a;
+        s_part[3 * wid + 1] = b;
+        s_part[3 * wid + 2] = __double_as_longlong(c);
+    }
     __syncthreads();
-    double t = 0.0;
-    for (int w = 0; w < NT / 32; ++w) t += s_part[w];
+    if (wid == 0) {
+        long long xa = 0, xb = 0, xc = 0;
+        if (lane < NW) {
+            xa = s_part[3 * lane];
+            xb = s_part[3 * lane + 1];
+            xc = s_part[3 * lane + 2];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            xa += __shfl_xor_sync(full, xa, o);
+            xb += __shfl_xor_sync(full, xb, o);
+        }
+        double dc = __longlong_as_double(xc);
+        if (__any_sync(full, xc != 0)) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) dc += __shfl_xor_sync(full, dc, o);
+        }
+        if (lane == 0) {
+            s_part[3 * NW] = xa;
+            s_part[3 * NW + 1] = xb;
+            s_part[3 * NW + 2] = __double_as_longlong(dc);
+        }
+    }
     __syncthreads();
-    return t;
+    a = s_part[3 * NW];
+    b = s_part[3 * NW + 1];
+    c = __longlong_as_double(s_part[3 * NW + 2]);
+    __syncthreads();
 }
 
-// Block-wide sum of one 64-bit value per thread (all threads get the total).
+// Block-wide sum of one 64-bit value per thread (all threads get the total);
+// same scheme and s_part size as block_sum3.
 template <int NT>
 __device__ __forceinline__ long long block_sum(long long v, long long* s_part)
 {
+    constexpr int NW = NT / 32;
+    static_assert(NW <= 32, "one warp adds the partials");
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(full, v, o);
     if (lane == 0) s_part[wid] = v;
     __syncthreads();
-    long long t = 0;
-#pragma unroll 4
-    for (int w = 0; w < NT / 32; ++w) t += s_part[w];
+    if (wid == 0) {
+        long long x = lane < NW ? s_part[lane] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(full, x, o);
+        if (lane == 0) s_part[3 * NW] = x;
+    }
+    __syncthreads();
+    const long long t = s_part[3 * NW];
     __syncthreads();
     return t;
 }

@@ -65,9 +65,9 @@ struct UpdSmem {
     LbSmem<NT> lb;
     int64_t dp[NT];
     double wn[NT];
-    double wo[NT];
+    double wd[NT];
     int fl[NT];
-    long long part[NT / 32];
+    long long part[3 * (NT / 32) + 3];
     int item, qt, at, st;
     int nscan, nprobe;  // level-2 vertices whose parents are found by scan / by probe
 };
@@ -98,6 +98,8 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         sm.qt = 1;
         sm.at = 0;
         sm.st = 0;
+        sm.nscan = 0;
+        sm.nprobe = 0;
     }
     __syncthreads();
 
@@ -150,11 +152,18 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
     __syncthreads();
 
     // ---------------- ascent ----------------
+    // A parent k's delta gains, per child x, sigma_k * (newdelta_x+1)/newsigma_x,
+    // and loses sigma_k * (olddelta_x+1)/oldsigma_x when k is not in the descent
+    // (k's sigma is then unchanged) -- except over the inserted edge (a, b),
+    // which had no old contribution.  acc[k] therefore sums the unscaled child
+    // weights wn = (newdelta+1)/newsigma or wd = wn - (olddelta+1)/oldsigma, and
+    // k's sigma multiplies the sum once, when k is committed: the walk over
+    // parent edges does no fp64 arithmetic (GB300's fp64 rate is a small
+    // fraction of its fp32 rate) and gathers no parent sigma.
     int L = 0;
     // Finalise vertex x of the level being walked: new sigma/delta committed in
-    // place, BC += newdelta - olddelta, and its push weights returned:
-    // wn = (newdelta+1)/newsigma, wo = (olddelta+1)/oldsigma.
-    auto commit = [&](int x, double& wn, double& wo) {
+    // place, BC += newdelta - olddelta, and its child weights wn, wd returned.
+    auto commit = [&](int x, double& wn, double& wd) {
         const int s = W.st[x];
         const bool isDown = (s & SBC_STEP_MASK) != 0;
         const bool mv = (s & SBC_MOVED) != 0;
@@ -162,24 +171,24 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         const double oD = Dl[x];
         const double ac = W.acc[x];
         const int64_t nS = isDown ? (mv ? W.dp[x] : oS + W.dp[x]) : oS;
-        const double nD = isDown ? ac : oD + ac;
+        const double nD = isDown ? (double)nS * ac : oD + (double)oS * ac;
         wn = (nD + 1.0) / (double)nS;
-        wo = oS ? (oD + 1.0) / (double)oS : 0.0;
+        wd = oS ? wn - (oD + 1.0) / (double)oS : wn;
         if (x != root) atomicAdd(&A.bc[x], nD - oD);
         S[x] = nS;
         Dl[x] = nD;
     };
     auto prep = [&](int j, int x, int d) {
-        double wn, wo;
-        commit(x, wn, wo);
+        double wn, wd;
+        commit(x, wn, wd);
         sm.wn[j] = wn;
-        sm.wo[j] = wo;
+        sm.wd[j] = wd;
         sm.fl[j] = ((W.st[x] & SBC_MOVED) ? 1 : 0) | (x == b ? 2 : 0);
     };
-    // Push weights of an already committed vertex, kept in its acc/dp slots.
+    // Child weights of an already committed vertex, kept in its acc/dp slots.
     auto prep_loaded = [&](int j, int x, int d) {
         sm.wn[j] = W.acc[x];
-        sm.wo[j] = __longlong_as_double((long long)W.dp[x]);
+        sm.wd[j] = __longlong_as_double((long long)W.dp[x]);
         sm.fl[j] = ((W.st[x] & SBC_MOVED) ? 1 : 0) | (x == b ? 2 : 0);
     };
     auto parent_edge = [&](int j, int x, int k, int dk) -> bool {
@@ -193,10 +202,8 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
                 W.qa[p] = k;
             }
         }
-        const int64_t nSk = kDown ? ((sk & SBC_MOVED) ? W.dp[k] : S[k] + W.dp[k]) : S[k];
-        double c = (double)nSk * sm.wn[j];
-        if (!kDown && !(k == a && (sm.fl[j] & 2))) c -= (double)S[k] * sm.wo[j];
-        atomicAdd(&W.acc[k], c);
+        const bool fresh = kDown || (k == a && (sm.fl[j] & 2));
+        atomicAdd(&W.acc[k], fresh ? sm.wn[j] : sm.wd[j]);
         return true;
     };
 
@@ -204,8 +211,8 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
     // be the root, and those of a level-2 vertex only the root's neighbours, so
     // instead of every walked vertex scanning its (often hub-sized) adjacency
     // for parents, each candidate parent y can scan its own adjacency for
-    // walked children c (dist = L and touched) and sum the same contributions
-    // newsigma[y]*wn[c] - [y ascent-only, (y,c) != (a,b)] sigma[y]*wo[c].  The
+    // walked children c (dist = L and touched) and sum the same child weights
+    // (wn[c] if y is in the descent or (y,c) = (a,b), else wd[c]).  The
     // cheaper direction is chosen per level by scanned-slot count; results are
     // the same either way.  Used only where no vertex of the level moved (no
     // same-level ex-parent rule applies).
@@ -217,19 +224,13 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
             A.G, g, D, D8, plist, pn, sm.lb, sm.wn, sm.fl,
             [&](int j, int y, int d) {
                 const int sy = W.st[y];
-                const bool yDown = (sy & SBC_STEP_MASK) != 0;
-                const int64_t oS = S[y];
-                sm.dp[j] = yDown ? ((sy & SBC_MOVED) ? W.dp[y] : oS + W.dp[y]) : oS;
-                sm.wo[j] = (double)oS;
-                sm.fl[j] = (yDown ? 1 : 0) | (y == a ? 2 : 0);
+                sm.fl[j] = ((sy & SBC_STEP_MASK) ? 1 : 0) | (y == a ? 2 : 0);
             },
             [&](int j, int y, int c, int, double& v) -> bool {
                 if (!((W.bits[c >> 5] >> (c & 31)) & 1u)) return false;
-                const double wn = W.acc[c];
-                const double wo = __longlong_as_double((long long)W.dp[c]);
-                v = (double)sm.dp[j] * wn;
                 const int fl = sm.fl[j];
-                if (!(fl & 1) && !((fl & 2) && c == b)) v -= sm.wo[j] * wo;
+                const bool fresh = (fl & 1) || ((fl & 2) && c == b);
+                v = fresh ? W.acc[c] : __longlong_as_double((long long)W.dp[c]);
                 return true;
             },
             [&](int j, int y) {
@@ -249,8 +250,9 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
 
     // Level-2 parents of each listed (committed) vertex x: every root
     // neighbour y (all at level 1) is looked up in x's sorted adjacency; a hit
-    // is a parent, which receives newsigma[y]*wn[x] - [y ascent-only,
-    // (y,x) != (a,b)] sigma[y]*wo[x] and is claimed.  Warp per x, lanes over y.
+    // is a parent, which receives x's child weight (wn[x] if y is in the
+    // descent or (y,x) = (a,b), else wd[x]) and is claimed.  Warp per x, lanes
+    // over y.
     auto probe_parents = [&](const int32_t* list, int n, int64_t rrow, int rdeg) {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         unsigned cost = 0;
@@ -259,7 +261,7 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
             const int64_t rx = A.G.row[x];
             const int vx = vis_deg(A.G, x, rx, g);
             const double wn = W.acc[x];
-            const double wo = __longlong_as_double((long long)W.dp[x]);
+            const double wd = __longlong_as_double((long long)W.dp[x]);
             for (int t = lane; t < rdeg; t += 32) {
                 const int y = A.G.col[rrow + t];
                 if (!has_edge(A.G, x, rx, vx, y, cost)) continue;
@@ -269,13 +271,10 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
                     int old = atomicOr(&W.st[y], SBC_ASC);
                     if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = y;
                 }
-                const int64_t nSy = yDown ? ((sy & SBC_MOVED) ? W.dp[y] : S[y] + W.dp[y]) : S[y];
-                double v = (double)nSy * wn;
-                if (!yDown && !(y == a && x == b)) v -= (double)S[y] * wo;
-                atomicAdd(&W.acc[y], v);
+                atomicAdd(&W.acc[y], (yDown || (y == a && x == b)) ? wn : wd);
             }
         }
-        atomicAdd(&sm.lb.scanned_e, (unsigned long long)cost);
+        if (cost) atomicAdd(&sm.lb.scanned_e, (unsigned long long)cost);
         __syncthreads();
     };
 
@@ -291,10 +290,19 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
         }
         const int next_lo = sm.at;
         const bool pull_ok = L >= 1 && L <= 2 && (!moving || L < Lb);
-        if (pull_ok || L == 0) {
+        if (L == 0) {
+            // The root alone (if reached): no parents, committing is all.
+            if (threadIdx.x == 0 && dn + ua_hi - ua_lo > 0) {
+                const int x = dn ? dlist[0] : W.qa[ua_lo];
+                double wn, wd;
+                commit(x, wn, wd);
+                sm.lb.walked_v += 1;
+                sm.lb.walked_e += (unsigned)vis_deg(A.G, x, A.G.row[x], g);
+            }
+            __syncthreads();
+        } else if (pull_ok) {
             // Commit every vertex x of the level and keep its push weights in
             // its acc/dp slots; count it as traversed (reference counters).
-            //   L == 0  the root alone: no parents, committing is all.
             //   L == 1  the only parent is the root (sigma 1): each x's
             //           contribution is summed straight into the root, no scan.
             //   L == 2  parents are N(x) ∩ N(root).  Per vertex, either scan
@@ -306,30 +314,20 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
             const int na_ = ua_hi - ua_lo;
             const int64_t rrow = A.G.row[root];
             const int rdeg = vis_deg(A.G, root, rrow, g);
-            const int rs = W.st[root];
-            const bool rootDown = (rs & SBC_STEP_MASK) != 0;
-            const double rS = (double)S[root];
-            const double rnS = rootDown ? (double)((rs & SBC_MOVED) ? W.dp[root] : S[root] + W.dp[root]) : rS;
-            if (threadIdx.x == 0) {
-                sm.nscan = 0;
-                sm.nprobe = 0;
-            }
-            __syncthreads();
+            const bool rootDown = (W.st[root] & SBC_STEP_MASK) != 0;
             long long push_cost = 0, mixed_cost = 0;
             double root_sum = 0.0;
             const int qbase = sm.st;  // free tail of the same-level queue holds the two lists
             for (int i = threadIdx.x; i < dn + na_; i += NT) {
                 const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
-                double wn, wo;
-                commit(x, wn, wo);
+                double wn, wd;
+                commit(x, wn, wd);
                 W.acc[x] = wn;
-                W.dp[x] = (int64_t)__double_as_longlong(wo);
+                W.dp[x] = (int64_t)__double_as_longlong(wd);
                 const int dx = vis_deg(A.G, x, A.G.row[x], g);
                 push_cost += dx;
                 if (L == 1) {
-                    double v = rnS * wn;
-                    if (!rootDown && !(root == a && x == b)) v -= rS * wo;
-                    root_sum += v;
+                    root_sum += (rootDown || (root == a && x == b)) ? wn : wd;
                 } else if (L == 2) {
                     atomicOr(&W.bits[x >> 5], 1u << (x & 31));
                     if ((long long)dx > (long long)kProbeRatio * rdeg) {
@@ -341,13 +339,12 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
                     }
                 }
             }
-            push_cost = block_sum<NT>(push_cost, sm.part);
+            block_sum3<NT>(push_cost, mixed_cost, root_sum, sm.part);
             if (threadIdx.x == 0) {
                 sm.lb.walked_v += (unsigned)(dn + na_);
                 sm.lb.walked_e += (unsigned long long)push_cost;
             }
             if (L == 1) {
-                root_sum = block_sum_f64<NT>(root_sum, (double*)sm.part);
                 if (threadIdx.x == 0 && dn + na_ > 0) {
                     W.acc[root] += root_sum;
                     if (!rootDown) {
@@ -357,7 +354,6 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
                 }
                 __syncthreads();
             } else if (L == 2 && dn + na_ > 0) {
-                mixed_cost = block_sum<NT>(mixed_cost, sm.part);
                 if (pull2_cost < 0) {
                     long long c = 0;
                     for (int i = threadIdx.x; i < rdeg; i += NT) {
@@ -400,7 +396,7 @@ __device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, co
                             W.qs[p] = k;
                         }
                     }
-                    atomicAdd(&W.acc[k], -(double)S[k] * sm.wo[j]);
+                    atomicAdd(&W.acc[k], sm.wd[j] - sm.wn[j]);
                 },
                 NoPost());
             const int same_hi = sm.st;

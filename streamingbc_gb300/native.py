@@ -10,6 +10,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import re
+import weakref
 
 import numpy as np
 
@@ -96,6 +97,7 @@ def load(path: str = LIB_PATH):
         "sbc_static_init": (C.c_int, [_vp]),
         "sbc_insert_batch": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
         "sbc_insert_batch_device": (C.c_int, [_vp, C.c_int64, _vp, _vp]),
+        "sbc_set_graph_capture": (C.c_int, [_vp, C.c_int]),
         "sbc_update_inserted": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
         "sbc_sync": (C.c_int, [_vp]),
         "sbc_read_counters": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
@@ -142,6 +144,7 @@ class DeviceGraph:
         _check(self.lib.sbc_graph_create(C.byref(h), int(nv), p64(self._off), p64(self._adj)))
         self.h = h
         self.nv = int(nv)
+        self._forests = weakref.WeakSet()
 
     def degree(self, v: int) -> int:
         d = C.c_int64()
@@ -172,6 +175,8 @@ class DeviceGraph:
         return off, adj
 
     def close(self):
+        for f in list(getattr(self, "_forests", ())):
+            f.close()  # forests first: they use the graph's stream
         if getattr(self, "h", None):
             self.lib.sbc_graph_destroy(self.h)
             self.h = None
@@ -196,6 +201,7 @@ class DeviceForest:
         self.h = h
         self.nv = graph.nv
         self.nk = int(self.roots.size)
+        graph._forests.add(self)
 
     def info(self) -> dict:
         v = [C.c_int64() for _ in range(4)]
@@ -218,6 +224,9 @@ class DeviceForest:
     def insert_device(self, n: int, d_u: int, d_v: int):
         """Asynchronous batch from int32 device pointers (e.g. tensor.data_ptr())."""
         _check(self.lib.sbc_insert_batch_device(self.h, int(n), _vp(d_u), _vp(d_v)))
+
+    def set_graph_capture(self, on: bool):
+        _check(self.lib.sbc_set_graph_capture(self.h, 1 if on else 0))
 
     def update_inserted(self, pairs) -> dict:
         pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)

@@ -283,16 +283,48 @@ def test_edge_cases_isolated_root_and_tiny_graphs(sbc_lib, port_lib):
     assert f1.dist().tolist() == [[0]] and f1.bc().tolist() == [0.0]
 
 
-def test_device_batch_entry_point(sbc_lib):
+@pytest.mark.parametrize("capture", [True, False])
+def test_device_batch_entry_point(sbc_lib, capture):
+    """Device-resident batches of 8: with capture on, the first batch is
+    captured as a CUDA graph and the next five replay it with re-pointed
+    inputs; with capture off every batch is launched directly."""
     torch = pytest.importorskip("torch")
     z = load_golden("rmat9")
     dg, f = make(int(z["nv"]), z["off"], z["adj"], z["roots"])
+    f.set_graph_capture(capture)
     f.static_init()
     dg.reserve(z["ins"])
     ins = torch.tensor(z["ins"], dtype=torch.int32, device="cuda")
     u = ins[:, 0].contiguous()
     v = ins[:, 1].contiguous()
     torch.cuda.synchronize()
-    f.insert_device(u.numel(), u.data_ptr(), v.data_ptr())
+    for s in range(0, u.numel(), 8):
+        f.insert_device(min(8, u.numel() - s), u[s:].data_ptr(), v[s:].data_ptr())
     f.sync()
     check_state(f, z["level1"], z["sigma1"], z["bc1"])
+
+
+def test_captured_batches_recaptured_after_repack(sbc_lib, port_lib):
+    """A re-pack moves the adjacency; replayed graphs must be re-captured."""
+    torch = pytest.importorskip("torch")
+    g = G.er(400, 800, seed=12)
+    roots = G.pick_roots(g.nv, 400, 0)
+    hub = 7
+    others = [w for w in range(g.nv) if w != hub and w not in set(g.adj[g.off[hub]:g.off[hub + 1]].tolist())]
+    ins = np.array([(hub, w) for w in others[:48]], dtype=np.int64)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    d = torch.tensor(ins, dtype=torch.int32, device="cuda")
+    u = d[:, 0].contiguous()
+    v = d[:, 1].contiguous()
+    torch.cuda.synchronize()
+    for s in range(0, len(ins), 8):
+        dg.reserve(ins[s:s + 8])          # slack of the hub runs out: re-packs happen between batches
+        f.insert_device(8, u[s:].data_ptr(), v[s:].data_ptr())
+        for a, b in ins[s:s + 8]:
+            o.insert(int(a), int(b))
+    f.sync()
+    assert dg.repacks() >= 2
+    check_state(f, o.level(), o.sigma(), o.bc())
