@@ -140,6 +140,24 @@ int sbc_insert_batch_device(sbc_forest *f, int64_t n, const int32_t *d_u, const 
  * either way. */
 int sbc_set_graph_capture(sbc_forest *f, int on);
 
+/* Launch-shape selection.  The reference picks its work split with the
+ * BALANCE/COARSE flags of insertEdgeStreamingBC (src/streamingbc.c:88-226,
+ * enums src/streamingbc.h:9-22); here the split is the update kernel's shape
+ * (threads per root, roots in flight per SM).  No shape changes any result.
+ * sbc_forest_set_variant re-sizes the worker scratch for shape `variant`
+ * (synchronous).  sbc_forest_autotune inserts the batch (u[i], v[i]) exactly
+ * like sbc_insert_batch, but first times the update of this same batch under
+ * every shape whose worker scratch fits in half the free memory, each on a
+ * fresh copy of the forest's state (reps runs, fastest kept; reps 0 = 2), and
+ * keeps the fastest shape for this and later batches.  ms[v] gets shape v's
+ * time in ms, -1 where skipped (ms may be NULL when ms_len is 0); *chosen the
+ * shape index (may be NULL).  The copy needs 21 B per root per vertex; when
+ * that does not fit in half the free memory a prefix of the roots is timed. */
+int sbc_forest_set_variant(sbc_forest *f, int variant);
+int sbc_forest_variant(const sbc_forest *f, int *variant);
+int sbc_forest_autotune(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, int reps, int *chosen,
+                        double *ms, int ms_len);
+
 /* Apply n insertions whose edges are ALREADY in the adjacency (inserted by
  * sbc_graph_insert_directed in both directions), exactly like
  * insertEdgeStreamingBC after the caller's stinger_insert_edge calls.

@@ -278,6 +278,76 @@ int check_graph_err(sbc_graph* g)
     return SBC_OK;
 }
 
+void free_scratch(sbc_forest* f)
+{
+    dev_free(f->d_st);
+    dev_free(f->d_dp);
+    dev_free(f->d_acc);
+    dev_free(f->d_qd);
+    dev_free(f->d_qa);
+    dev_free(f->d_qs);
+    dev_free(f->d_lvl);
+    dev_free(f->d_bits);
+    f->workers = 0;
+    f->bytes = f->state_bytes;
+}
+
+void drop_captured(sbc_forest* f)
+{
+    for (auto& p : f->captured)
+        if (p.second.exec) cudaGraphExecDestroy(p.second.exec);
+    f->captured.clear();
+}
+
+// Scratch bytes of one persistent worker: st, qd, qa, qs (4 B), dp, acc (8 B)
+// and lvl (4 B) per vertex, plus one bitmap bit per vertex.
+size_t scratch_per_worker(int64_t nv) { return (size_t)nv * 36 + sbc::bitmap_words(nv) * 4 + 16; }
+
+// Worker count of launch shape `variant`: one per CTA the update kernel keeps
+// resident (or the caller's count), at most one per root, and at most as many
+// as half of `free_b` holds.
+int64_t workers_for(const sbc_forest* f, int variant, size_t free_b)
+{
+    int per_sm = sbc::update_workers_per_sm(variant);
+    if (per_sm < 1) per_sm = 1;
+    int64_t w = f->workers_req > 0 ? f->workers_req : (int64_t)per_sm * f->sm_count;
+    const int64_t fit = (int64_t)((free_b / 2) / scratch_per_worker(f->nv));
+    w = std::min<int64_t>(w, std::max<int64_t>(fit, 1));
+    w = std::min<int64_t>(w, f->nk);
+    return std::max<int64_t>(w, 1);
+}
+
+// (Re)allocates the persistent workers' scratch for launch shape `variant`
+// and zeroes it (every job leaves the scratch it touched zeroed again).  The
+// static kernel runs over the same worker slots.  Captured batch graphs hold
+// the old shape, so they are dropped.
+int alloc_scratch(sbc_forest* f, int variant)
+{
+    sbc_graph* g = f->g;
+    free_scratch(f);
+    drop_captured(f);
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const int64_t w = workers_for(f, variant, free_b);
+    const size_t words = sbc::bitmap_words(f->nv);
+    const size_t sc = (size_t)w * (size_t)f->nv;
+    cudaError_t e;
+    if ((e = dev_alloc(&f->d_st, sc)) || (e = dev_alloc(&f->d_dp, sc)) || (e = dev_alloc(&f->d_acc, sc)) ||
+        (e = dev_alloc(&f->d_qd, sc)) || (e = dev_alloc(&f->d_qa, sc)) || (e = dev_alloc(&f->d_qs, sc)) ||
+        (e = dev_alloc(&f->d_lvl, (size_t)w * (size_t)(f->nv + 2))) || (e = dev_alloc(&f->d_bits, (size_t)w * words))) {
+        free_scratch(f);
+        return cuda_fail(e, "worker scratch allocation");
+    }
+    f->variant = variant;
+    f->workers = w;
+    f->bytes = f->state_bytes + (int64_t)(sc * 36 + (size_t)w * words * 4);
+    CK(cudaMemsetAsync(f->d_bits, 0, sizeof(uint32_t) * (size_t)w * words, g->stream));
+    CK(cudaMemsetAsync(f->d_st, 0, sizeof(int32_t) * sc, g->stream));
+    CK(cudaMemsetAsync(f->d_dp, 0, sizeof(int64_t) * sc, g->stream));
+    CK(cudaMemsetAsync(f->d_acc, 0, sizeof(double) * sc, g->stream));
+    return SBC_OK;
+}
+
 template <class T>
 int get_rows(sbc_forest* f, const T* base, int64_t r0, int64_t nr, T* out)
 {
@@ -532,36 +602,13 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
         return cuda_fail(e, "sbc_forest_create state allocation");
     }
     f->d_counter = f->d_nwork + 1;
-    f->bytes = (int64_t)(cells * 21 + f->nv * 8);
-
-    // Persistent workers: as many as the update kernel keeps resident, and
-    // their scratch (36 B + 1 bit per vertex each) limited to half of the
-    // memory still free.  The static kernel runs over the same worker slots.
-    int per_sm = sbc::update_workers_per_sm(variant);
-    if (per_sm < 1) per_sm = 1;
-    int64_t w = workers > 0 ? workers : (int64_t)per_sm * f->sm_count;
-    const size_t words = sbc::bitmap_words(f->nv);
-    const size_t per_worker = (size_t)f->nv * 36 + words * 4 + 16;
-    size_t free_b = 0, total_b = 0;
-    cudaMemGetInfo(&free_b, &total_b);
-    int64_t fit = (int64_t)((free_b / 2) / per_worker);
-    w = std::min<int64_t>(w, std::max<int64_t>(fit, 1));
-    w = std::min<int64_t>(w, nk);
-    w = std::max<int64_t>(w, 1);
-    f->workers = w;
-    const size_t sc = (size_t)w * (size_t)f->nv;
-    if ((e = dev_alloc(&f->d_st, sc)) || (e = dev_alloc(&f->d_dp, sc)) || (e = dev_alloc(&f->d_acc, sc)) ||
-        (e = dev_alloc(&f->d_qd, sc)) || (e = dev_alloc(&f->d_qa, sc)) || (e = dev_alloc(&f->d_qs, sc)) ||
-        (e = dev_alloc(&f->d_lvl, (size_t)w * (size_t)(f->nv + 2))) ||
-        (e = dev_alloc(&f->d_bits, (size_t)w * words))) {
+    f->state_bytes = (int64_t)(cells * 21 + f->nv * 8);
+    f->workers_req = workers;
+    int rc = alloc_scratch(f, variant);
+    if (rc) {
         sbc_forest_destroy(f);
-        return cuda_fail(e, "sbc_forest_create scratch allocation");
+        return rc;
     }
-    f->bytes += (int64_t)(sc * 36 + (size_t)w * words * 4);
-    CK(cudaMemsetAsync(f->d_bits, 0, sizeof(uint32_t) * (size_t)w * words, g->stream));
-    CK(cudaMemsetAsync(f->d_st, 0, sizeof(int32_t) * sc, g->stream));
-    CK(cudaMemsetAsync(f->d_dp, 0, sizeof(int64_t) * sc, g->stream));
-    CK(cudaMemsetAsync(f->d_acc, 0, sizeof(double) * sc, g->stream));
     CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
     CK(cudaMemcpyAsync(f->d_roots, roots, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, g->stream));
     CK(f->prof_init());
@@ -591,17 +638,9 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_worklist);
     dev_free(f->d_nwork);
     dev_free(f->d_counters);
-    dev_free(f->d_st);
-    dev_free(f->d_dp);
-    dev_free(f->d_acc);
-    dev_free(f->d_qd);
-    dev_free(f->d_qa);
-    dev_free(f->d_qs);
-    dev_free(f->d_lvl);
-    dev_free(f->d_bits);
+    free_scratch(f);
     f->prof_release();
-    for (auto& p : f->captured)
-        if (p.second.exec) cudaGraphExecDestroy(p.second.exec);
+    drop_captured(f);
     if (f->t0) cudaEventDestroy(f->t0);
     if (f->t1) cudaEventDestroy(f->t1);
     delete f;
@@ -685,6 +724,148 @@ int sbc_set_graph_capture(sbc_forest* f, int on)
     if (!f) return fail(SBC_ERR_ARG, "sbc_set_graph_capture: null");
     f->use_graphs = on != 0;
     return SBC_OK;
+}
+
+int sbc_forest_set_variant(sbc_forest* f, int variant)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_forest_set_variant: the forest's graph was destroyed");
+    if (!f) return fail(SBC_ERR_ARG, "sbc_forest_set_variant: null");
+    if (variant < 0 || variant >= sbc::update_variant_count())
+        return fail(SBC_ERR_ARG, "update variant %d out of range", variant);
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    if (variant == f->variant && f->workers > 0) return SBC_OK;
+    CK(cudaStreamSynchronize(f->g->stream));
+    int rc = alloc_scratch(f, variant);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(f->g->stream));
+    return SBC_OK;
+}
+
+int sbc_forest_variant(const sbc_forest* f, int* variant)
+{
+    if (!f || !variant) return fail(SBC_ERR_ARG, "sbc_forest_variant: null");
+    *variant = f->variant;
+    return SBC_OK;
+}
+
+int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, int reps, int* chosen,
+                        double* ms, int ms_len)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_forest_autotune: the forest's graph was destroyed");
+    if (!f || n <= 0 || !u || !v || reps < 0 || ms_len < 0 || (ms_len > 0 && !ms))
+        return fail(SBC_ERR_ARG, "sbc_forest_autotune: bad arguments");
+    if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_forest_autotune before sbc_static_init");
+    if (n >= INT32_MAX) return fail(SBC_ERR_ARG, "batch too large");
+    sbc_graph* g = f->g;
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    if (reps == 0) reps = 2;
+    const int nvar = sbc::update_variant_count();
+    for (int i = 0; i < ms_len; ++i) ms[i] = -1.0;
+    int rc = plan_capacity(g, n, u, v, false);
+    if (rc) return rc;
+    if ((rc = stage_host(g, n, u, v, false))) return rc;
+    CK(sbc::launch_append(g, (int)n, false));
+    CK(cudaStreamSynchronize(g->stream));
+
+    // Trial copy of the state: all roots if it fits in half the free memory,
+    // else a prefix of the (uniformly drawn) roots.
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t row_bytes = (size_t)f->nv * 21;
+    int64_t nk_t = std::min<int64_t>(f->nk, (int64_t)((free_b / 2) / row_bytes));
+    if (nk_t < 1) return fail(SBC_ERR_CUDA, "sbc_forest_autotune: no memory for a trial copy of one root");
+    const size_t cells = (size_t)nk_t * (size_t)f->nv;
+    int32_t* t_dist = nullptr;
+    uint8_t* t_dist8 = nullptr;
+    int64_t* t_sigma = nullptr;
+    double *t_delta = nullptr, *t_bc = nullptr;
+    unsigned long long saved_counters[SBC_NCOUNTERS];
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const bool prof = f->prof;
+    const int64_t nk = f->nk;
+    const int old_variant = f->variant;
+    int best = -1;
+    double best_ms = 0.0;
+    cudaError_t e;
+    auto swap_state = [&]() {
+        std::swap(f->d_dist, t_dist);
+        std::swap(f->d_dist8, t_dist8);
+        std::swap(f->d_sigma, t_sigma);
+        std::swap(f->d_delta, t_delta);
+        std::swap(f->d_bc, t_bc);
+    };
+    auto cleanup = [&]() {
+        dev_free(t_dist);
+        dev_free(t_dist8);
+        dev_free(t_sigma);
+        dev_free(t_delta);
+        dev_free(t_bc);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        f->prof = prof;
+        f->nk = nk;
+    };
+    if ((e = dev_alloc(&t_dist, cells)) || (e = dev_alloc(&t_dist8, cells)) || (e = dev_alloc(&t_sigma, cells)) ||
+        (e = dev_alloc(&t_delta, cells)) || (e = dev_alloc(&t_bc, f->nv)) || (e = cudaEventCreate(&e0)) ||
+        (e = cudaEventCreate(&e1)) ||
+        (e = cudaMemcpyAsync(saved_counters, f->d_counters, sizeof saved_counters, cudaMemcpyDeviceToHost, g->stream)) ||
+        (e = cudaStreamSynchronize(g->stream))) {
+        cleanup();
+        return cuda_fail(e, "sbc_forest_autotune setup");
+    }
+    f->prof = false;
+    for (int c = 0; c < nvar; ++c) {
+        CK(cudaMemGetInfo(&free_b, &total_b));
+        // a shape runs only with its full worker count, so that its time is its own
+        const int per_sm = std::max(1, sbc::update_workers_per_sm(c));
+        const int64_t want = std::min<int64_t>(f->workers_req > 0 ? f->workers_req : (int64_t)per_sm * f->sm_count, nk);
+        const size_t have = free_b + (size_t)std::max<int64_t>(f->workers, 0) * scratch_per_worker(f->nv);
+        if ((size_t)want * scratch_per_worker(f->nv) > have / 2) continue;
+        if ((rc = alloc_scratch(f, c))) {
+            cleanup();
+            return rc;
+        }
+        double c_ms = -1.0;
+        for (int rep = 0; rep < reps; ++rep) {
+            const size_t bytes_cells = cells;
+            if ((e = cudaMemcpyAsync(t_dist, f->d_dist, sizeof(int32_t) * bytes_cells, cudaMemcpyDeviceToDevice, g->stream)) ||
+                (e = cudaMemcpyAsync(t_dist8, f->d_dist8, bytes_cells, cudaMemcpyDeviceToDevice, g->stream)) ||
+                (e = cudaMemcpyAsync(t_sigma, f->d_sigma, sizeof(int64_t) * bytes_cells, cudaMemcpyDeviceToDevice, g->stream)) ||
+                (e = cudaMemcpyAsync(t_delta, f->d_delta, sizeof(double) * bytes_cells, cudaMemcpyDeviceToDevice, g->stream)) ||
+                (e = cudaMemcpyAsync(t_bc, f->d_bc, sizeof(double) * f->nv, cudaMemcpyDeviceToDevice, g->stream))) {
+                cleanup();
+                return cuda_fail(e, "sbc_forest_autotune trial copy");
+            }
+            swap_state();
+            f->nk = nk_t;
+            e = cudaEventRecord(e0, g->stream);
+            if (!e) e = sbc::launch_update(f, (int)n, false);
+            if (!e) e = cudaEventRecord(e1, g->stream);
+            f->nk = nk;
+            swap_state();
+            if (!e) e = cudaEventSynchronize(e1);
+            float t = 0.f;
+            if (!e) e = cudaEventElapsedTime(&t, e0, e1);
+            if (e) {
+                cleanup();
+                return cuda_fail(e, "sbc_forest_autotune trial");
+            }
+            if (c_ms < 0.0 || t < c_ms) c_ms = t;
+        }
+        if (c < ms_len) ms[c] = c_ms;
+        if (best < 0 || c_ms < best_ms) {
+            best = c;
+            best_ms = c_ms;
+        }
+    }
+    cleanup();
+    if (best < 0) best = old_variant;
+    if ((rc = alloc_scratch(f, best))) return rc;
+    CK(cudaMemcpyAsync(f->d_counters, saved_counters, sizeof saved_counters, cudaMemcpyHostToDevice, g->stream));
+    CK(sbc::launch_update(f, (int)n, false));
+    CK(sbc::launch_seal(g, (int)n));
+    if (chosen) *chosen = best;
+    return check_graph_err(g);
 }
 
 int sbc_update_inserted(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, sbc_batch_stats* stats)

@@ -75,6 +75,8 @@ struct sbc_forest {
     int sm_count = 0;
     int variant = 0;  // launch shape of the update kernel
     int64_t workers = 0;
+    int64_t workers_req = 0;  // worker count the caller asked for (0 = one per resident CTA)
+    int64_t state_bytes = 0;
     int32_t* d_st = nullptr;
     int64_t* d_dp = nullptr;
     double* d_acc = nullptr;

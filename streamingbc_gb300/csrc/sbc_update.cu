@@ -523,6 +523,10 @@ static const UpdateVariant kVariants[] = {
     {512, 2, launch_variant<512, 2>, occupancy_variant<512, 2>},
     {512, 1, launch_variant<512, 1>, occupancy_variant<512, 1>},
     {1024, 1, launch_variant<1024, 1>, occupancy_variant<1024, 1>},
+    // one or two warps per root (coarse grain): many roots in flight, for
+    // graphs whose per-root touched sets are a few hundred vertices
+    {64, 16, launch_variant<64, 16>, occupancy_variant<64, 16>},
+    {32, 32, launch_variant<32, 32>, occupancy_variant<32, 32>},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 // 1024 threads x 1 CTA per SM measured fastest on R-MAT scale 20, K = 1024

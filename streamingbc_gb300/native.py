@@ -98,6 +98,10 @@ def load(path: str = LIB_PATH):
         "sbc_insert_batch": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
         "sbc_insert_batch_device": (C.c_int, [_vp, C.c_int64, _vp, _vp]),
         "sbc_set_graph_capture": (C.c_int, [_vp, C.c_int]),
+        "sbc_forest_set_variant": (C.c_int, [_vp, C.c_int]),
+        "sbc_forest_variant": (C.c_int, [_vp, C.POINTER(C.c_int)]),
+        "sbc_forest_autotune": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.c_int, C.POINTER(C.c_int), _f64p,
+                                          C.c_int]),
         "sbc_update_inserted": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
         "sbc_sync": (C.c_int, [_vp]),
         "sbc_read_counters": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
@@ -227,6 +231,32 @@ class DeviceForest:
 
     def set_graph_capture(self, on: bool):
         _check(self.lib.sbc_set_graph_capture(self.h, 1 if on else 0))
+
+    @property
+    def variant(self) -> int:
+        v = C.c_int(0)
+        _check(self.lib.sbc_forest_variant(self.h, C.byref(v)))
+        return v.value
+
+    def set_variant(self, variant: int):
+        """Re-size the worker scratch for update launch shape `variant`."""
+        _check(self.lib.sbc_forest_set_variant(self.h, int(variant)))
+
+    def autotune(self, pairs, reps: int = 2):
+        """Insert the batch `pairs` after timing its update under every launch
+        shape that fits (on copies of the state); the fastest shape is kept.
+        Returns (chosen shape, per-shape ms with -1 for skipped shapes)."""
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        u = np.ascontiguousarray(pairs[:, 0])
+        v = np.ascontiguousarray(pairs[:, 1])
+        n = C.c_int(0)
+        _check(self.lib.sbc_update_variant_count(C.byref(n)))
+        ms = np.full(n.value, -1.0)
+        chosen = C.c_int(-1)
+        _check(self.lib.sbc_forest_autotune(self.h, len(u), p64(u), p64(v), int(reps), C.byref(chosen),
+                                            ms.ctypes.data_as(_f64p),
+                                            n.value))
+        return chosen.value, ms
 
     def update_inserted(self, pairs) -> dict:
         pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)

@@ -328,3 +328,58 @@ def test_captured_batches_recaptured_after_repack(sbc_lib, port_lib):
     f.sync()
     assert dg.repacks() >= 2
     check_state(f, o.level(), o.sigma(), o.bc())
+
+
+@pytest.mark.parametrize("case", ["er1024"])
+def test_autotune_keeps_results_and_picks_fastest(sbc_lib, port_lib, case):
+    """The tuner's batch is applied exactly once (its timing runs work on
+    copies), later batches run in the chosen shape, and the state matches the
+    oracle after each batch; the chosen shape is the fastest one timed."""
+    g, roots, ins = G.workload(case)
+    ins = ins[:192]
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    for s in range(0, len(ins), 64):
+        for u, v in ins[s:s + 64]:
+            o.insert(int(u), int(v))
+        if s == 0:
+            chosen, ms = f.autotune(ins[s:s + 64], reps=1)
+            timed = ms >= 0
+            assert timed.sum() >= 2 and timed[chosen]
+            assert ms[chosen] == ms[timed].min()
+            assert f.variant == chosen
+        else:
+            f.insert(ins[s:s + 64])
+        check_state(f, o.level(), o.sigma(), o.bc())
+    f.close()
+    dg.close()
+
+
+def test_switching_shapes_between_batches(sbc_lib, port_lib):
+    """Re-sizing the worker scratch between batches (device batches replayed
+    from captured graphs included) never changes results."""
+    import ctypes
+    import torch
+    n = ctypes.c_int()
+    sbc_lib.sbc_update_variant_count(ctypes.byref(n))
+    g, roots, ins = G.workload("chunglu40k")
+    ins = ins[:32 * n.value]
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    dg.reserve(ins)
+    f.static_init()
+    d = torch.tensor(ins, dtype=torch.int32, device="cuda")
+    u, v = d[:, 0].contiguous(), d[:, 1].contiguous()
+    for k in range(n.value):
+        f.set_variant(n.value - 1 - k)
+        s = 32 * k
+        for a, b in ins[s:s + 32]:
+            o.insert(int(a), int(b))
+        f.insert_device(32, u[s:].data_ptr(), v[s:].data_ptr())
+        f.sync()
+        check_state(f, o.level(), o.sigma(), o.bc())
+    f.close()
+    dg.close()
