@@ -44,8 +44,11 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["rmat20", "rmat18", "rmat16", "chunglu40k", "er1024"], default="rmat20")
+    p.add_argument("--workload", choices=["rmat20", "rmat18", "rmat16", "chunglu40k", "er1024", "rmat_group64"],
+                   default="rmat20")
     p.add_argument("--batch", type=int, default=64)
+    p.add_argument("--group-batch", type=int, default=16,
+                   help="rmat_group64: insertions per graph per step (64 graphs per step)")
     p.add_argument("--plain", type=int, default=16, help="insertions timed on the plain one-at-a-time path")
     p.add_argument("--cpu-roots", type=int, default=0, help="roots in the CPU sample (0 = 2 x host threads)")
     p.add_argument("--cpu-insertions", type=int, default=16)
@@ -201,11 +204,57 @@ def cpu_sample(g, roots, ins, n_roots, n_ins, threads):
             "static_sample_s": t_static}
 
 
+GROUP_WORKLOAD = "rmat_group64"
+GROUP_DESC = ("rmat_group64: 64 independent R-MAT graphs, scales uniform in 10..16 (drawn with seed 100), edge "
+              "factor 8, a/b/c/d .57/.19/.19/.05, seeds 100..163, symmetrised+deduplicated; K=min(|V|,128) uniform "
+              "roots each; R-MAT-drawn new-edge insertions, {b} per graph per step, all 64 graphs in one group batch")
+
+
+def cpu_sample_group(specs, batch, n_ins, threads):
+    """Oracle port on every graph of the group: min(K, 2*threads) roots and
+    the first n_ins insertions per graph; a group step's CPU time is the sum
+    over graphs of batch x (per-root time x K/n_roots + BC reduce)."""
+    from oracle import oracle as orc
+    orc.build()
+    total = 0.0
+    per_graph = []
+    for g, roots, ins, _ in specs:
+        nr = min(len(roots), 2 * threads)
+        o = orc.PortOracle(g.nv, g.off, g.adj, roots[:nr], nthreads=threads)
+        o.static_timed()
+        per = []
+        for u, v in ins[:n_ins]:
+            tr, tb = o.insert_timed(int(u), int(v))
+            per.append(tr * (len(roots) / nr) + tb)
+        o.close()
+        per_graph.append(float(np.mean(per)))
+        total += batch * per_graph[-1]
+    value = len(specs) * batch / total
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"every graph: min(K, {2 * threads}) roots, first {n_ins} insertions; per-root time scaled "
+                      f"to K, BC reduce added per insertion; step = {batch} insertions on each of {len(specs)} graphs",
+            "per_graph_insertion_ms_mean": float(np.mean(per_graph)) * 1e3}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
+    if args.workload == GROUP_WORKLOAD:
+        from streamingbc_gb300 import graphs as G
+        specs = G.rmat_group(insertions=max(512, args.warmup + args.steps))
+        cpu = cpu_sample_group(specs, args.group_batch, max(args.warmup + args.steps, 4), threads)
+        value = cpu["value"]
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": len(specs) * args.group_batch / value * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64",
+                "data": "synthetic", "impl": "reference",
+                "config": {"workload": GROUP_DESC.format(b=args.group_batch), "graphs": len(specs)},
+                "cpu_baseline": cpu,
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     need = args.warmup + args.steps
     g, roots, ins = load_workload(args.workload, need)
     n_roots = args.cpu_roots or min(len(roots), 2 * threads)
@@ -232,6 +281,123 @@ def run_reference(args):
                                        f"x{len(roots) / n_roots:g}, BC reduce added once"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_group(args):
+    """64 R-MAT graphs updated together: one group batch (append, classify,
+    update, seal over all graphs) per step."""
+    rank, world, local = dist_env()
+    import torch
+    from streamingbc_gb300 import build as b
+    from streamingbc_gb300 import graphs as G
+    from streamingbc_gb300 import native
+    if not os.path.exists(native.LIB_PATH):
+        b.build()
+    lib = native.load()
+    lib.sbc_set_device(local if world > 1 else 0)
+    torch.cuda.set_device(local if world > 1 else 0)
+    B = args.group_batch
+    n_val = (args.warmup + args.steps) * B
+    n_e2e = 0 if args.no_e2e else (1 + args.steps) * B
+    t0 = time.time()
+    specs = G.rmat_group(insertions=max(512, n_val + n_e2e))
+    gen_s = time.time() - t0
+    objs = []
+    t0 = time.time()
+    for g, roots, ins, _ in specs:
+        dg = native.DeviceGraph(g.nv, g.off, g.adj)
+        f = native.DeviceForest(dg, roots, workers=1)
+        dg.reserve(ins[:n_val + n_e2e])
+        f.static_init()
+        objs.append((dg, f))
+    for _, f in objs:
+        f.sync()
+    static_s = time.time() - t0
+    grp = native.DeviceGroup([f for _, f in objs], variant=args.variant)
+
+    def batches(s):
+        return [ins[s * B:(s + 1) * B] for _, _, ins, _ in specs]
+
+    tuned = None
+    w0 = 0
+    if args.variant < 0 and args.warmup > 0:
+        chosen, tms = grp.autotune(batches(0), reps=2)
+        tuned = {"chosen": chosen, "ms_per_shape": [round(float(x), 3) for x in tms]}
+        w0 = 1
+    for s in range(w0, args.warmup):
+        grp.insert(batches(s))
+    grp.counters()
+    clk = ClockSampler(local)
+    clk.start()
+    torch.cuda.synchronize()
+    dev_ms = []
+    t_wall = time.perf_counter()
+    for s in range(args.warmup, args.warmup + args.steps):
+        dev_ms.append(grp.insert(batches(s)))
+    wall_ms = (time.perf_counter() - t_wall) * 1e3
+    clocks = clk.stop()
+    cnt = grp.counters()
+    n_step = B * len(specs)
+    total_ms = float(np.sum(dev_ms))
+    value = args.steps * n_step / (total_ms / 1e3)
+    K = sum(len(r) for _, r, _, _ in specs)
+    alg_bytes = 8 * cnt["scanned"] + 40 * cnt["vertices"] + 16 * K * B * args.steps
+    achieved = alg_bytes / (total_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+
+    e2e = None
+    if n_e2e:
+        base = n_val // B
+        grp.insert(batches(base))
+        for _, f in objs:
+            f.bc()
+        lat = []
+        t1 = time.perf_counter()
+        for s in range(base + 1, base + 1 + args.steps):
+            ts = time.perf_counter()
+            grp.insert(batches(s))
+            for _, f in objs:
+                f.bc()
+            lat.append((time.perf_counter() - ts) * 1e3)
+        e2e_s = time.perf_counter() - t1
+        nv_sum = sum(g.nv for g, _, _, _ in specs)
+        e2e = {"value": args.steps * n_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 4 * n_step,
+               "d2h_bytes_per_step": 8 * nv_sum + 4 * len(specs),
+               "p50_step_ms": float(np.percentile(lat, 50)), "p99_step_ms": float(np.percentile(lat, 99))}
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        cpu = cpu_sample_group(specs, B, args.cpu_insertions // 2 or 4, os.cpu_count() or 1)
+    info = grp.info()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64+f64", "data": "synthetic",
+            "config": {"workload": GROUP_DESC.format(b=B), "graphs": len(specs), "roots": K,
+                       "vertices": sum(g.nv for g, _, _, _ in specs), "batch_per_graph": B,
+                       "parallelism": "single GPU", "variant": info["variant"], "workers": info["workers"],
+                       "autotune": tuned, "static_init_s": static_s, "generate_s": gen_s,
+                       "l2": "per-root state of all graphs on device; no flush (inputs change every step)",
+                       "timing": "CUDA events on the group stream around each batch's append..seal launches"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "kernel": "k_update_group (whole batch sequence timed)",
+                         "alg_bytes_per_launch": alg_bytes / args.steps,
+                         "avg_launch_ms": total_ms / args.steps},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clocks,
+            "gpu_launches": 4 * args.steps,  # append, classify, update, seal per group batch
+            "latency_ms": {"batch_p50": float(np.percentile(dev_ms, 50)), "wall_ms_timed": wall_ms},
+            "work": {"traversed_vertices": cnt["vertices"], "traversed_edges": cnt["edges"],
+                     "scanned_slots": cnt["scanned"], "case1_pairs": cnt["case1"], "case2_pairs": cnt["case2"],
+                     "insertions": args.steps * n_step},
+        }
+        print(json.dumps(line), flush=True)
+    grp.close()
+    for dg, f in objs:
+        f.close()
+        dg.close()
 
 
 def run_ours(args):
@@ -427,6 +593,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == GROUP_WORKLOAD:
+        run_group(args)
     else:
         run_ours(args)
 

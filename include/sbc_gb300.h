@@ -36,6 +36,7 @@ extern "C" {
 
 typedef struct sbc_graph sbc_graph;
 typedef struct sbc_forest sbc_forest;
+typedef struct sbc_group sbc_group;
 
 /* Per-call statistics of an insertion batch (counters match the reference's
  * COUNT_TRAVERSALS counters, src/streamingbc_internal.c:107-110,203-206,
@@ -163,6 +164,32 @@ int sbc_forest_autotune(sbc_forest *f, int64_t n, const int64_t *u, const int64_
  * insertEdgeStreamingBC after the caller's stinger_insert_edge calls.
  * Synchronous; stats may be NULL. */
 int sbc_update_inserted(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, sbc_batch_stats *stats);
+
+/* ---- groups: many forests updated by one launch per batch --------------
+ * The reference updates one forest per insertEdgeStreamingBC call
+ * (src/streamingbc.c:88-226); a group applies one batch to each of up to 64
+ * forests, each over its own graph, with one append, one classify and one
+ * persistent update launch whose work items are (forest, root) pairs from a
+ * single queue.  Results equal those of per-forest sbc_insert_batch calls.
+ * The group has its own stream and worker scratch; work queued on the members'
+ * graph streams is ordered before and after each group batch.  A member
+ * forest cannot be destroyed while a group holding it is alive. */
+int sbc_group_create(sbc_group **out, int n, sbc_forest *const *forests, int variant /* -1: by size */);
+int sbc_group_destroy(sbc_group *G);
+int sbc_group_info(const sbc_group *G, int *n, int64_t *workers, int64_t *bytes, int *variant);
+int sbc_group_set_variant(sbc_group *G, int variant);
+/* counts[i] insertions for forests[i] (creation order); u/v hold them
+ * concatenated in that order.  Synchronous; device_ms (may be NULL) receives
+ * the device time of the batch's append..seal launches. */
+int sbc_group_insert_batch(sbc_group *G, const int64_t *counts, const int64_t *u, const int64_t *v,
+                           double *device_ms);
+/* As sbc_group_insert_batch, after timing the update of this batch under every
+ * launch shape that fits, on copies of all members' state (see
+ * sbc_forest_autotune); the fastest shape is kept. */
+int sbc_group_autotune(sbc_group *G, const int64_t *counts, const int64_t *u, const int64_t *v, int reps,
+                       int *chosen, double *ms, int ms_len);
+int sbc_group_read_counters(sbc_group *G, int64_t *vertices, int64_t *edges, int64_t *case1, int64_t *case2,
+                            int64_t *scanned);
 
 /* Wait for all work queued on the forest's graph stream. */
 int sbc_sync(sbc_forest *f);

@@ -280,14 +280,7 @@ int check_graph_err(sbc_graph* g)
 
 void free_scratch(sbc_forest* f)
 {
-    dev_free(f->d_st);
-    dev_free(f->d_dp);
-    dev_free(f->d_acc);
-    dev_free(f->d_qd);
-    dev_free(f->d_qa);
-    dev_free(f->d_qs);
-    dev_free(f->d_lvl);
-    dev_free(f->d_bits);
+    f->ws.release();
     f->workers = 0;
     f->bytes = f->state_bytes;
 }
@@ -299,9 +292,7 @@ void drop_captured(sbc_forest* f)
     f->captured.clear();
 }
 
-// Scratch bytes of one persistent worker: st, qd, qa, qs (4 B), dp, acc (8 B)
-// and lvl (4 B) per vertex, plus one bitmap bit per vertex.
-size_t scratch_per_worker(int64_t nv) { return (size_t)nv * 36 + sbc::bitmap_words(nv) * 4 + 16; }
+size_t scratch_per_worker(int64_t nv) { return WorkerScratch::per_worker(nv); }
 
 // Worker count of launch shape `variant`: one per CTA the update kernel keeps
 // resident (or the caller's count), at most one per root, and at most as many
@@ -329,23 +320,139 @@ int alloc_scratch(sbc_forest* f, int variant)
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     const int64_t w = workers_for(f, variant, free_b);
-    const size_t words = sbc::bitmap_words(f->nv);
-    const size_t sc = (size_t)w * (size_t)f->nv;
-    cudaError_t e;
-    if ((e = dev_alloc(&f->d_st, sc)) || (e = dev_alloc(&f->d_dp, sc)) || (e = dev_alloc(&f->d_acc, sc)) ||
-        (e = dev_alloc(&f->d_qd, sc)) || (e = dev_alloc(&f->d_qa, sc)) || (e = dev_alloc(&f->d_qs, sc)) ||
-        (e = dev_alloc(&f->d_lvl, (size_t)w * (size_t)(f->nv + 2))) || (e = dev_alloc(&f->d_bits, (size_t)w * words))) {
+    cudaError_t e = f->ws.alloc(w, f->nv, g->stream);
+    if (e) {
         free_scratch(f);
         return cuda_fail(e, "worker scratch allocation");
     }
     f->variant = variant;
     f->workers = w;
-    f->bytes = f->state_bytes + (int64_t)(sc * 36 + (size_t)w * words * 4);
-    CK(cudaMemsetAsync(f->d_bits, 0, sizeof(uint32_t) * (size_t)w * words, g->stream));
-    CK(cudaMemsetAsync(f->d_st, 0, sizeof(int32_t) * sc, g->stream));
-    CK(cudaMemsetAsync(f->d_dp, 0, sizeof(int64_t) * sc, g->stream));
-    CK(cudaMemsetAsync(f->d_acc, 0, sizeof(double) * sc, g->stream));
+    f->bytes = f->state_bytes + (int64_t)f->ws.bytes();
     return SBC_OK;
+}
+
+// A copy of the first nk rows of a forest's state (and its BC) that an
+// autotuner's timing runs work on: swap() exchanges it with the forest's own
+// arrays, so a launch between two swaps updates the copy only.
+struct TrialState {
+    int64_t nk = 0;
+    int32_t* dist = nullptr;
+    uint8_t* dist8 = nullptr;
+    int64_t* sigma = nullptr;
+    double* delta = nullptr;
+    double* bc = nullptr;
+    cudaError_t alloc(const sbc_forest* f, int64_t rows)
+    {
+        nk = rows;
+        const size_t cells = (size_t)rows * (size_t)f->nv;
+        cudaError_t e;
+        if ((e = dev_alloc(&dist, cells)) || (e = dev_alloc(&dist8, cells)) || (e = dev_alloc(&sigma, cells)) ||
+            (e = dev_alloc(&delta, cells)) || (e = dev_alloc(&bc, f->nv)))
+            release();
+        return e;
+    }
+    void release()
+    {
+        dev_free(dist);
+        dev_free(dist8);
+        dev_free(sigma);
+        dev_free(delta);
+        dev_free(bc);
+    }
+    cudaError_t copy_from(const sbc_forest* f, cudaStream_t s) const
+    {
+        const size_t cells = (size_t)nk * (size_t)f->nv;
+        const auto d2d = cudaMemcpyDeviceToDevice;
+        cudaError_t e;
+        if ((e = cudaMemcpyAsync(dist, f->d_dist, sizeof(int32_t) * cells, d2d, s)) ||
+            (e = cudaMemcpyAsync(dist8, f->d_dist8, cells, d2d, s)) ||
+            (e = cudaMemcpyAsync(sigma, f->d_sigma, sizeof(int64_t) * cells, d2d, s)) ||
+            (e = cudaMemcpyAsync(delta, f->d_delta, sizeof(double) * cells, d2d, s)) ||
+            (e = cudaMemcpyAsync(bc, f->d_bc, sizeof(double) * f->nv, d2d, s)))
+            return e;
+        return cudaSuccess;
+    }
+    void swap(sbc_forest* f)
+    {
+        std::swap(f->d_dist, dist);
+        std::swap(f->d_dist8, dist8);
+        std::swap(f->d_sigma, sigma);
+        std::swap(f->d_delta, delta);
+        std::swap(f->d_bc, bc);
+        std::swap(f->nk, nk);
+    }
+};
+
+// ---- groups ----
+
+void group_free_scratch(sbc_group* G) { G->ws.release(); }
+
+// Worker scratch of the group for shape `variant`: one worker per resident
+// CTA, at most one per root of all members, within half the free memory.
+int group_alloc_scratch(sbc_group* G, int variant)
+{
+    G->ws.release();
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const int per_sm = std::max(1, sbc::group_workers_per_sm(variant));
+    int64_t w = (int64_t)per_sm * G->sm_count;
+    w = std::min<int64_t>(w, std::max<int64_t>((int64_t)((free_b / 2) / WorkerScratch::per_worker(G->nv_max)), 1));
+    w = std::max<int64_t>(std::min<int64_t>(w, G->total_roots), 1);
+    cudaError_t e = G->ws.alloc(w, G->nv_max, G->stream);
+    if (e) return cuda_fail(e, "group worker scratch allocation");
+    G->variant = variant;
+    return SBC_OK;
+}
+
+// Work queued on the members' graph streams precedes what is queued next on
+// the group's stream, and vice versa.
+int group_after_members(sbc_group* G)
+{
+    for (sbc_forest* f : G->members) {
+        CK(cudaEventRecord(G->ev, f->g->stream));
+        CK(cudaStreamWaitEvent(G->stream, G->ev, 0));
+    }
+    return SBC_OK;
+}
+
+int members_after_group(sbc_group* G)
+{
+    CK(cudaEventRecord(G->ev, G->stream));
+    for (sbc_forest* f : G->members) CK(cudaStreamWaitEvent(f->g->stream, G->ev, 0));
+    return SBC_OK;
+}
+
+// Validates the per-member counts (caller order), plans slack and stages each
+// member's insertions in its graph; counts_slot[s] receives slot s's count.
+int group_stage(sbc_group* G, const int64_t* counts, const int64_t* u, const int64_t* v, std::vector<int>& counts_slot)
+{
+    const int ns = (int)G->members.size();
+    std::vector<int64_t> off(ns + 1, 0);
+    for (int i = 0; i < ns; ++i) {
+        if (counts[i] < 0 || counts[i] >= INT32_MAX) return fail(SBC_ERR_ARG, "group batch: bad count for member %d", i);
+        off[i + 1] = off[i] + counts[i];
+    }
+    if (off[ns] > 0 && (!u || !v)) return fail(SBC_ERR_ARG, "group batch: null endpoints");
+    counts_slot.assign(ns, 0);
+    for (int s = 0; s < ns; ++s) {
+        const int m = G->order[s];
+        const int64_t n = counts[m];
+        counts_slot[s] = (int)n;
+        if (n == 0) continue;
+        sbc_graph* g = G->members[s]->g;
+        int rc = plan_capacity(g, n, u + off[m], v + off[m], false);
+        if (rc) return rc;
+        if ((rc = stage_host(g, n, u + off[m], v + off[m], false))) return rc;
+    }
+    return SBC_OK;
+}
+
+int group_check(sbc_group* G)
+{
+    if (!G) return fail(SBC_ERR_ARG, "group: null");
+    for (sbc_forest* f : G->members)
+        if (!f->g) return fail(SBC_ERR_STATE, "group: a member's graph was destroyed");
+    return use_device(G->device);
 }
 
 template <class T>
@@ -623,6 +730,7 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
 int sbc_forest_destroy(sbc_forest* f)
 {
     if (!f) return SBC_OK;
+    if (f->groups > 0) return fail(SBC_ERR_STATE, "sbc_forest_destroy: the forest is a member of a live group");
     use_device(f->device);
     if (f->g) {
         cudaStreamSynchronize(f->g->stream);
@@ -771,43 +879,23 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
     // else a prefix of the (uniformly drawn) roots.
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
-    const size_t row_bytes = (size_t)f->nv * 21;
-    int64_t nk_t = std::min<int64_t>(f->nk, (int64_t)((free_b / 2) / row_bytes));
+    const int64_t nk_t = std::min<int64_t>(f->nk, (int64_t)((free_b / 2) / ((size_t)f->nv * 21)));
     if (nk_t < 1) return fail(SBC_ERR_CUDA, "sbc_forest_autotune: no memory for a trial copy of one root");
-    const size_t cells = (size_t)nk_t * (size_t)f->nv;
-    int32_t* t_dist = nullptr;
-    uint8_t* t_dist8 = nullptr;
-    int64_t* t_sigma = nullptr;
-    double *t_delta = nullptr, *t_bc = nullptr;
+    TrialState T;
     unsigned long long saved_counters[SBC_NCOUNTERS];
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     const bool prof = f->prof;
-    const int64_t nk = f->nk;
     const int old_variant = f->variant;
     int best = -1;
     double best_ms = 0.0;
     cudaError_t e;
-    auto swap_state = [&]() {
-        std::swap(f->d_dist, t_dist);
-        std::swap(f->d_dist8, t_dist8);
-        std::swap(f->d_sigma, t_sigma);
-        std::swap(f->d_delta, t_delta);
-        std::swap(f->d_bc, t_bc);
-    };
     auto cleanup = [&]() {
-        dev_free(t_dist);
-        dev_free(t_dist8);
-        dev_free(t_sigma);
-        dev_free(t_delta);
-        dev_free(t_bc);
+        T.release();
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
         f->prof = prof;
-        f->nk = nk;
     };
-    if ((e = dev_alloc(&t_dist, cells)) || (e = dev_alloc(&t_dist8, cells)) || (e = dev_alloc(&t_sigma, cells)) ||
-        (e = dev_alloc(&t_delta, cells)) || (e = dev_alloc(&t_bc, f->nv)) || (e = cudaEventCreate(&e0)) ||
-        (e = cudaEventCreate(&e1)) ||
+    if ((e = T.alloc(f, nk_t)) || (e = cudaEventCreate(&e0)) || (e = cudaEventCreate(&e1)) ||
         (e = cudaMemcpyAsync(saved_counters, f->d_counters, sizeof saved_counters, cudaMemcpyDeviceToHost, g->stream)) ||
         (e = cudaStreamSynchronize(g->stream))) {
         cleanup();
@@ -818,8 +906,8 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
         CK(cudaMemGetInfo(&free_b, &total_b));
         // a shape runs only with its full worker count, so that its time is its own
         const int per_sm = std::max(1, sbc::update_workers_per_sm(c));
-        const int64_t want = std::min<int64_t>(f->workers_req > 0 ? f->workers_req : (int64_t)per_sm * f->sm_count, nk);
-        const size_t have = free_b + (size_t)std::max<int64_t>(f->workers, 0) * scratch_per_worker(f->nv);
+        const int64_t want = std::min<int64_t>(f->workers_req > 0 ? f->workers_req : (int64_t)per_sm * f->sm_count, f->nk);
+        const size_t have = free_b + f->ws.bytes();
         if ((size_t)want * scratch_per_worker(f->nv) > have / 2) continue;
         if ((rc = alloc_scratch(f, c))) {
             cleanup();
@@ -827,22 +915,15 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
         }
         double c_ms = -1.0;
         for (int rep = 0; rep < reps; ++rep) {
-            const size_t bytes_cells = cells;
-            if ((e = cudaMemcpyAsync(t_dist, f->d_dist, sizeof(int32_t) * bytes_cells, cudaMemcpyDeviceToDevice, g->stream)) ||
-                (e = cudaMemcpyAsync(t_dist8, f->d_dist8, bytes_cells, cudaMemcpyDeviceToDevice, g->stream)) ||
-                (e = cudaMemcpyAsync(t_sigma, f->d_sigma, sizeof(int64_t) * bytes_cells, cudaMemcpyDeviceToDevice, g->stream)) ||
-                (e = cudaMemcpyAsync(t_delta, f->d_delta, sizeof(double) * bytes_cells, cudaMemcpyDeviceToDevice, g->stream)) ||
-                (e = cudaMemcpyAsync(t_bc, f->d_bc, sizeof(double) * f->nv, cudaMemcpyDeviceToDevice, g->stream))) {
+            if ((e = T.copy_from(f, g->stream))) {
                 cleanup();
                 return cuda_fail(e, "sbc_forest_autotune trial copy");
             }
-            swap_state();
-            f->nk = nk_t;
+            T.swap(f);
             e = cudaEventRecord(e0, g->stream);
             if (!e) e = sbc::launch_update(f, (int)n, false);
             if (!e) e = cudaEventRecord(e1, g->stream);
-            f->nk = nk;
-            swap_state();
+            T.swap(f);
             if (!e) e = cudaEventSynchronize(e1);
             float t = 0.f;
             if (!e) e = cudaEventElapsedTime(&t, e0, e1);
@@ -866,6 +947,225 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
     CK(sbc::launch_seal(g, (int)n));
     if (chosen) *chosen = best;
     return check_graph_err(g);
+}
+
+// ------------------------------------------------------------------ groups
+
+int sbc_group_create(sbc_group** out, int n, sbc_forest* const* forests, int variant)
+{
+    if (!out || n < 1 || !forests) return fail(SBC_ERR_ARG, "sbc_group_create: bad arguments");
+    *out = nullptr;
+    if (n > sbc::kMaxGroup) return fail(SBC_ERR_ARG, "sbc_group_create: at most %d forests", sbc::kMaxGroup);
+    if (variant >= sbc::group_variant_count()) return fail(SBC_ERR_ARG, "update variant %d out of range", variant);
+    int64_t total = 0, nv_max = 0;
+    for (int i = 0; i < n; ++i) {
+        sbc_forest* f = forests[i];
+        if (!f || !f->g) return fail(SBC_ERR_ARG, "sbc_group_create: forest %d is null or lost its graph", i);
+        if (f->device != forests[0]->device) return fail(SBC_ERR_ARG, "sbc_group_create: forests on different devices");
+        for (int j = 0; j < i; ++j)
+            if (forests[j] == f || forests[j]->g == f->g)
+                return fail(SBC_ERR_ARG, "sbc_group_create: forests %d and %d share a forest or a graph", j, i);
+        if (f->nk >= (int64_t)1 << 25) return fail(SBC_ERR_ARG, "sbc_group_create: forest %d has too many roots", i);
+        total += f->nk;
+        nv_max = std::max<int64_t>(nv_max, f->nv);
+    }
+    if (total >= INT32_MAX) return fail(SBC_ERR_ARG, "sbc_group_create: too many roots in total");
+    if (use_device(forests[0]->device)) return SBC_ERR_CUDA;
+    sbc_group* G = new sbc_group();
+    G->device = forests[0]->device;
+    G->nv_max = nv_max;
+    G->total_roots = total;
+    G->sm_count = forests[0]->sm_count;
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+        return forests[a]->nk * forests[a]->nv > forests[b]->nk * forests[b]->nv;
+    });
+    for (int s = 0; s < n; ++s) {
+        G->order.push_back(idx[s]);
+        G->members.push_back(forests[idx[s]]);
+    }
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking)) ||
+        (e = cudaEventCreateWithFlags(&G->ev, cudaEventDisableTiming)) || (e = cudaEventCreate(&G->t0)) ||
+        (e = cudaEventCreate(&G->t1)) || (e = dev_alloc(&G->d_worklist, (size_t)total)) ||
+        (e = dev_alloc(&G->d_nwork, 2)) || (e = dev_alloc(&G->d_counters, SBC_NCOUNTERS)) ||
+        (e = cudaMemsetAsync(G->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, G->stream))) {
+        sbc_group_destroy(G);
+        return cuda_fail(e, "sbc_group_create");
+    }
+    if (variant < 0) variant = nv_max <= 8192 ? 3 : (nv_max <= 262144 ? 5 : sbc::update_default_variant());
+    int rc = group_alloc_scratch(G, variant);
+    if (rc) {
+        sbc_group_destroy(G);
+        return rc;
+    }
+    CK(cudaStreamSynchronize(G->stream));
+    for (sbc_forest* f : G->members) f->groups++;
+    *out = G;
+    return SBC_OK;
+}
+
+int sbc_group_destroy(sbc_group* G)
+{
+    if (!G) return SBC_OK;
+    use_device(G->device);
+    if (G->stream) cudaStreamSynchronize(G->stream);
+    for (sbc_forest* f : G->members) f->groups--;
+    group_free_scratch(G);
+    dev_free(G->d_worklist);
+    dev_free(G->d_nwork);
+    dev_free(G->d_counters);
+    if (G->ev) cudaEventDestroy(G->ev);
+    if (G->t0) cudaEventDestroy(G->t0);
+    if (G->t1) cudaEventDestroy(G->t1);
+    if (G->stream) cudaStreamDestroy(G->stream);
+    delete G;
+    return SBC_OK;
+}
+
+int sbc_group_info(const sbc_group* G, int* n, int64_t* workers, int64_t* bytes, int* variant)
+{
+    if (!G) return fail(SBC_ERR_ARG, "sbc_group_info: null");
+    if (n) *n = (int)G->members.size();
+    if (workers) *workers = G->ws.workers;
+    if (bytes) *bytes = (int64_t)G->ws.bytes() + G->total_roots * 4;
+    if (variant) *variant = G->variant;
+    return SBC_OK;
+}
+
+int sbc_group_set_variant(sbc_group* G, int variant)
+{
+    int rc = group_check(G);
+    if (rc) return rc;
+    if (variant < 0 || variant >= sbc::group_variant_count())
+        return fail(SBC_ERR_ARG, "update variant %d out of range", variant);
+    CK(cudaStreamSynchronize(G->stream));
+    if ((rc = group_alloc_scratch(G, variant))) return rc;
+    CK(cudaStreamSynchronize(G->stream));
+    return SBC_OK;
+}
+
+int sbc_group_insert_batch(sbc_group* G, const int64_t* counts, const int64_t* u, const int64_t* v, double* device_ms)
+{
+    int rc = group_check(G);
+    if (rc) return rc;
+    if (!counts) return fail(SBC_ERR_ARG, "sbc_group_insert_batch: null counts");
+    for (sbc_forest* f : G->members)
+        if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_group_insert_batch before sbc_static_init of a member");
+    std::vector<int> cs;
+    if ((rc = group_stage(G, counts, u, v, cs))) return rc;
+    if ((rc = group_after_members(G))) return rc;
+    CK(cudaEventRecord(G->t0, G->stream));
+    CK(sbc::launch_group_update(G, cs.data(), sbc::GROUP_ALL));
+    CK(cudaEventRecord(G->t1, G->stream));
+    if ((rc = members_after_group(G))) return rc;
+    CK(cudaStreamSynchronize(G->stream));
+    if (device_ms) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, G->t0, G->t1));
+        *device_ms = t;
+    }
+    for (sbc_forest* f : G->members)
+        if ((rc = check_graph_err(f->g))) return rc;
+    return SBC_OK;
+}
+
+int sbc_group_autotune(sbc_group* G, const int64_t* counts, const int64_t* u, const int64_t* v, int reps, int* chosen,
+                       double* ms, int ms_len)
+{
+    int rc = group_check(G);
+    if (rc) return rc;
+    if (!counts || reps < 0 || ms_len < 0 || (ms_len > 0 && !ms))
+        return fail(SBC_ERR_ARG, "sbc_group_autotune: bad arguments");
+    for (sbc_forest* f : G->members)
+        if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_group_autotune before sbc_static_init of a member");
+    if (reps == 0) reps = 2;
+    for (int i = 0; i < ms_len; ++i) ms[i] = -1.0;
+    std::vector<int> cs;
+    if ((rc = group_stage(G, counts, u, v, cs))) return rc;
+    if ((rc = group_after_members(G))) return rc;
+    CK(sbc::launch_group_update(G, cs.data(), sbc::GROUP_APPEND));
+    CK(cudaStreamSynchronize(G->stream));
+    // trial copies of every member's full state
+    const int ns = (int)G->members.size();
+    std::vector<TrialState> T(ns);
+    size_t need = 0, free_b = 0, total_b = 0;
+    for (sbc_forest* f : G->members) need += (size_t)f->nk * (size_t)f->nv * 21 + (size_t)f->nv * 8;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const bool can_time = need <= free_b / 2;
+    unsigned long long saved[SBC_NCOUNTERS];
+    CK(cudaMemcpy(saved, G->d_counters, sizeof saved, cudaMemcpyDeviceToHost));
+    int best = G->variant;
+    double best_ms = -1.0;
+    cudaError_t e = cudaSuccess;
+    auto release = [&]() {
+        for (auto& t : T) t.release();
+    };
+    for (int s = 0; can_time && s < ns && !e; ++s) e = T[s].alloc(G->members[s], G->members[s]->nk);
+    if (e) {
+        release();
+        return cuda_fail(e, "sbc_group_autotune trial copies");
+    }
+    for (int c = 0; can_time && c < sbc::group_variant_count(); ++c) {
+        CK(cudaMemGetInfo(&free_b, &total_b));
+        const int per_sm = std::max(1, sbc::group_workers_per_sm(c));
+        const int64_t want = std::min<int64_t>((int64_t)per_sm * G->sm_count, G->total_roots);
+        if ((size_t)want * WorkerScratch::per_worker(G->nv_max) > (free_b + G->ws.bytes()) / 2) continue;
+        if ((rc = group_alloc_scratch(G, c))) {
+            release();
+            return rc;
+        }
+        double c_ms = -1.0;
+        for (int rep = 0; rep < reps; ++rep) {
+            for (int s = 0; s < ns && !e; ++s) e = T[s].copy_from(G->members[s], G->stream);
+            for (int s = 0; s < ns; ++s) T[s].swap(G->members[s]);
+            if (!e) e = cudaEventRecord(G->t0, G->stream);
+            if (!e) e = sbc::launch_group_update(G, cs.data(), sbc::GROUP_UPDATE);
+            if (!e) e = cudaEventRecord(G->t1, G->stream);
+            for (int s = 0; s < ns; ++s) T[s].swap(G->members[s]);
+            if (!e) e = cudaEventSynchronize(G->t1);
+            float t = 0.f;
+            if (!e) e = cudaEventElapsedTime(&t, G->t0, G->t1);
+            if (e) {
+                release();
+                return cuda_fail(e, "sbc_group_autotune trial");
+            }
+            if (c_ms < 0.0 || t < c_ms) c_ms = t;
+        }
+        if (c < ms_len) ms[c] = c_ms;
+        if (best_ms < 0.0 || c_ms < best_ms) {
+            best = c;
+            best_ms = c_ms;
+        }
+    }
+    release();
+    if (best != G->variant && (rc = group_alloc_scratch(G, best))) return rc;
+    CK(cudaMemcpyAsync(G->d_counters, saved, sizeof saved, cudaMemcpyHostToDevice, G->stream));
+    CK(sbc::launch_group_update(G, cs.data(), sbc::GROUP_UPDATE | sbc::GROUP_SEAL));
+    if ((rc = members_after_group(G))) return rc;
+    CK(cudaStreamSynchronize(G->stream));
+    if (chosen) *chosen = best;
+    for (sbc_forest* f : G->members)
+        if ((rc = check_graph_err(f->g))) return rc;
+    return SBC_OK;
+}
+
+int sbc_group_read_counters(sbc_group* G, int64_t* vertices, int64_t* edges, int64_t* case1, int64_t* case2,
+                            int64_t* scanned)
+{
+    int rc = group_check(G);
+    if (rc) return rc;
+    unsigned long long c[SBC_NCOUNTERS];
+    CK(cudaMemcpyAsync(c, G->d_counters, sizeof c, cudaMemcpyDeviceToHost, G->stream));
+    CK(cudaMemsetAsync(G->d_counters, 0, sizeof c, G->stream));
+    CK(cudaStreamSynchronize(G->stream));
+    if (vertices) *vertices = (int64_t)c[0];
+    if (edges) *edges = (int64_t)c[1];
+    if (case1) *case1 = (int64_t)c[2];
+    if (case2) *case2 = (int64_t)c[3];
+    if (scanned) *scanned = (int64_t)c[4];
+    return SBC_OK;
 }
 
 int sbc_update_inserted(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, sbc_batch_stats* stats)

@@ -14,9 +14,10 @@ namespace sbc {
 // Insertion outcome codes written to ok[i]:
 //   1 inserted, 0 duplicate (edge already present), -1 self loop or id out of
 //   range, -2 no slack left (the host plans capacity so this is not expected).
-__global__ void k_append(int64_t nv, const int64_t* __restrict__ row, int32_t* deg, const int32_t* __restrict__ cap,
-                         int32_t* col, int32_t* seq, int n, const int32_t* __restrict__ iu,
-                         const int32_t* __restrict__ iv, int32_t* ok, int directed, int* err)
+__device__ __forceinline__ void append_warp(int64_t nv, const int64_t* __restrict__ row, int32_t* deg,
+                                            const int32_t* __restrict__ cap, int32_t* col, int32_t* seq, int n,
+                                            const int32_t* __restrict__ iu, const int32_t* __restrict__ iv,
+                                            int32_t* ok, int directed, int* err)
 {
     const int lane = threadIdx.x;
     for (int i = 0; i < n; ++i) {
@@ -57,6 +58,21 @@ __global__ void k_append(int64_t nv, const int64_t* __restrict__ row, int32_t* d
         }
         __syncwarp();
     }
+}
+
+__global__ void k_append(int64_t nv, const int64_t* __restrict__ row, int32_t* deg, const int32_t* __restrict__ cap,
+                         int32_t* col, int32_t* seq, int n, const int32_t* __restrict__ iu,
+                         const int32_t* __restrict__ iv, int32_t* ok, int directed, int* err)
+{
+    append_warp(nv, row, deg, cap, col, seq, n, iu, iv, ok, directed, err);
+}
+
+// Many graphs' batches at once: one warp (CTA) per graph, each appending its
+// graph's insertions in order exactly as k_append does.
+__global__ void k_append_group(const __grid_constant__ GraphBatchSlots S)
+{
+    const GraphBatchSlot& b = S.slot[blockIdx.x];
+    append_warp(b.nv, b.row, b.deg, b.cap, b.col, b.seq, b.n, b.iu, b.iv, b.ok, 0, b.err);
 }
 
 // A batch's endpoint arrays live in the caller's device memory.  k_set_src
@@ -104,6 +120,16 @@ __global__ void k_seal(int n, const int32_t* __restrict__ iu, const int32_t* __r
     deg0[iv[i]] = deg[iv[i]];
 }
 
+// k_seal over many graphs: blockIdx.y selects the graph.
+__global__ void k_seal_group(const __grid_constant__ GraphBatchSlots S)
+{
+    const GraphBatchSlot& b = S.slot[blockIdx.y];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.n || b.ok[i] <= 0) return;
+    b.deg0[b.iu[i]] = b.deg[b.iu[i]];
+    b.deg0[b.iv[i]] = b.deg[b.iv[i]];
+}
+
 // Copy every vertex's live slots to a new layout with larger slack (warp per vertex).
 __global__ void k_repack(int64_t nv, const int64_t* __restrict__ orow, const int32_t* __restrict__ deg,
                          const int32_t* __restrict__ ocol, const int32_t* __restrict__ oseq,
@@ -137,6 +163,40 @@ cudaError_t launch_seal(sbc_graph* g, int n)
     const int32_t* iv = g->d_ins + g->ins_capacity;
     const int32_t* ok = g->d_ins + 2 * g->ins_capacity;
     k_seal<<<(n + 255) / 256, 256, 0, g->stream>>>(n, iu, iv, ok, g->d_deg, g->d_deg0);
+    return cudaGetLastError();
+}
+
+GraphBatchSlot graph_batch_slot(sbc_graph* g, int n)
+{
+    GraphBatchSlot b;
+    b.nv = g->nv;
+    b.row = g->d_row;
+    b.deg = g->d_deg;
+    b.deg0 = g->d_deg0;
+    b.cap = g->d_cap;
+    b.col = g->d_col;
+    b.seq = g->d_seq;
+    b.iu = g->d_ins;
+    b.iv = g->d_ins + g->ins_capacity;
+    b.ok = g->d_ins + 2 * g->ins_capacity;
+    b.err = g->d_err;
+    b.n = n;
+    return b;
+}
+
+cudaError_t launch_append_group(const GraphBatchSlots& S, cudaStream_t s)
+{
+    if (S.count <= 0) return cudaSuccess;
+    k_append_group<<<S.count, 32, 0, s>>>(S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seal_group(const GraphBatchSlots& S, cudaStream_t s)
+{
+    int nmax = 0;
+    for (int i = 0; i < S.count; ++i) nmax = std::max(nmax, S.slot[i].n);
+    if (S.count <= 0 || nmax <= 0) return cudaSuccess;
+    k_seal_group<<<dim3((nmax + 255) / 256, S.count), 256, 0, s>>>(S);
     return cudaGetLastError();
 }
 

@@ -16,6 +16,69 @@ enum ProfKernel { PROF_STATIC = 0, PROF_APPEND, PROF_CLASSIFY, PROF_UPDATE, PROF
 
 struct sbc_forest;
 
+// Scratch of a set of persistent update/static workers, each sized for nv
+// vertices: step/state word, queues and level offsets (int32), diffPath
+// (int64), delta accumulator (fp64) and one bitmap bit per vertex.  Zeroed on
+// allocation; every job leaves what it touched zeroed again.
+struct WorkerScratch {
+    int64_t workers = 0, nv = 0;
+    int32_t* st = nullptr;
+    int64_t* dp = nullptr;
+    double* acc = nullptr;
+    int32_t* qd = nullptr;
+    int32_t* qa = nullptr;
+    int32_t* qs = nullptr;
+    int32_t* lvl = nullptr;
+    uint32_t* bits = nullptr;
+
+    static size_t per_worker(int64_t nv) { return (size_t)nv * 36 + sbc::bitmap_words(nv) * 4 + 16; }
+    size_t bytes() const
+    {
+        return (size_t)workers * ((size_t)nv * 36 + (size_t)8 + sbc::bitmap_words(nv) * 4);
+    }
+    void release()
+    {
+        for (void* p : {(void*)st, (void*)dp, (void*)acc, (void*)qd, (void*)qa, (void*)qs, (void*)lvl, (void*)bits})
+            if (p) cudaFree(p);
+        st = qd = qa = qs = lvl = nullptr;
+        dp = nullptr;
+        acc = nullptr;
+        bits = nullptr;
+        workers = 0;
+    }
+    cudaError_t alloc(int64_t w, int64_t n, cudaStream_t s)
+    {
+        release();
+        const size_t sc = (size_t)w * (size_t)n, words = (size_t)w * sbc::bitmap_words(n);
+        cudaError_t e;
+        if ((e = cudaMalloc(&st, sc * 4)) || (e = cudaMalloc(&dp, sc * 8)) || (e = cudaMalloc(&acc, sc * 8)) ||
+            (e = cudaMalloc(&qd, sc * 4)) || (e = cudaMalloc(&qa, sc * 4)) || (e = cudaMalloc(&qs, sc * 4)) ||
+            (e = cudaMalloc(&lvl, (size_t)w * (size_t)(n + 2) * 4)) || (e = cudaMalloc(&bits, words * 4))) {
+            release();
+            return e;
+        }
+        workers = w;
+        nv = n;
+        if ((e = cudaMemsetAsync(st, 0, sc * 4, s)) || (e = cudaMemsetAsync(dp, 0, sc * 8, s)) ||
+            (e = cudaMemsetAsync(acc, 0, sc * 8, s)) || (e = cudaMemsetAsync(bits, 0, words * 4, s)))
+            return e;
+        return cudaSuccess;
+    }
+    sbc::ScratchBase base() const
+    {
+        sbc::ScratchBase b;
+        b.st = st;
+        b.dp = dp;
+        b.acc = acc;
+        b.qd = qd;
+        b.qa = qa;
+        b.qs = qs;
+        b.lvl = lvl;
+        b.bits = bits;
+        return b;
+    }
+};
+
 // Device-resident slack-CSR adjacency (replaces the STINGER edge-block store,
 // src/stinger/stinger-internal.h:45-103).  All device work for the graph and
 // for forests bound to it runs on `stream`, in order.
@@ -74,17 +137,11 @@ struct sbc_forest {
     // persistent workers and their scratch
     int sm_count = 0;
     int variant = 0;  // launch shape of the update kernel
-    int64_t workers = 0;
+    int64_t workers = 0;      // == ws.workers
     int64_t workers_req = 0;  // worker count the caller asked for (0 = one per resident CTA)
+    int groups = 0;           // groups this forest is a member of
     int64_t state_bytes = 0;
-    int32_t* d_st = nullptr;
-    int64_t* d_dp = nullptr;
-    double* d_acc = nullptr;
-    int32_t* d_qd = nullptr;
-    int32_t* d_qa = nullptr;
-    int32_t* d_qs = nullptr;
-    int32_t* d_lvl = nullptr;
-    uint32_t* d_bits = nullptr;
+    WorkerScratch ws;
     int* d_worklist = nullptr;
     int* d_nwork = nullptr;   // [1]
     int* d_counter = nullptr; // [1]
@@ -115,19 +172,7 @@ struct sbc_forest {
     int64_t prof_n[sbc::PROF_COUNT] = {};
     cudaEvent_t t0 = nullptr, t1 = nullptr;
 
-    sbc::ScratchBase scratch() const
-    {
-        sbc::ScratchBase s;
-        s.st = d_st;
-        s.dp = d_dp;
-        s.acc = d_acc;
-        s.qd = d_qd;
-        s.qa = d_qa;
-        s.qs = d_qs;
-        s.lvl = d_lvl;
-        s.bits = d_bits;
-        return s;
-    }
+    sbc::ScratchBase scratch() const { return ws.base(); }
     cudaError_t prof_init()
     {
         for (int k = 0; k < sbc::PROF_COUNT; ++k) {
@@ -183,7 +228,74 @@ struct sbc_forest {
     }
 };
 
+// Forests over different graphs updated together: one append, classify and
+// persistent update launch per batch on the group's own stream, with the
+// group's own worker scratch (stride: the largest member's vertex count).
+// members[s] is slot s (largest roots x vertices first); order[s] is the
+// index the caller gave that member.
+struct sbc_group {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<sbc_forest*> members;
+    std::vector<int> order;
+    int sm_count = 0;
+    int variant = 0;
+    int64_t nv_max = 0, total_roots = 0;
+    WorkerScratch ws;
+    uint32_t* d_worklist = nullptr;
+    int* d_nwork = nullptr;  // [2]: nwork, work counter
+    unsigned long long* d_counters = nullptr;  // [SBC_NCOUNTERS]
+    cudaEvent_t ev = nullptr;                  // stream hand-off
+    cudaEvent_t t0 = nullptr, t1 = nullptr;    // device time of the last batch
+};
+
 namespace sbc {
+// Most forests (and graphs) one group launch takes.
+constexpr int kMaxGroup = 64;
+
+// One graph's staged batch as the group append and seal kernels see it.
+struct GraphBatchSlot {
+    int64_t nv;
+    const int64_t* row;
+    int32_t* deg;
+    int32_t* deg0;
+    const int32_t* cap;
+    int32_t* col;
+    int32_t* seq;
+    const int32_t* iu;
+    const int32_t* iv;
+    int32_t* ok;
+    int* err;
+    int n;
+};
+struct GraphBatchSlots {
+    GraphBatchSlot slot[kMaxGroup];
+    int count;
+};
+GraphBatchSlot graph_batch_slot(sbc_graph* g, int n);
+cudaError_t launch_append_group(const GraphBatchSlots& S, cudaStream_t s);
+cudaError_t launch_seal_group(const GraphBatchSlots& S, cudaStream_t s);
+
+// Device view of forest f with the n insertions staged in its graph.
+inline ForestSlot forest_slot(const sbc_forest* f, int n)
+{
+    const sbc_graph* g = f->g;
+    ForestSlot s;
+    s.G = g->dev();
+    s.roots = f->d_roots;
+    s.dist = f->d_dist;
+    s.dist8 = f->d_dist8;
+    s.sigma = f->d_sigma;
+    s.delta = f->d_delta;
+    s.bc = f->d_bc;
+    s.ins_u = g->d_ins;
+    s.ins_v = g->d_ins + g->ins_capacity;
+    s.ins_ok = g->d_ins + 2 * g->ins_capacity;
+    s.nins = n;
+    s.nk = (int)f->nk;
+    return s;
+}
+
 int static_workers_per_sm();
 int update_variant_count();
 int update_default_variant();
@@ -200,4 +312,10 @@ cudaError_t launch_set_src(sbc_graph* g, const int32_t* d_u, const int32_t* d_v)
 cudaError_t launch_stage(sbc_graph* g, int n);
 cudaError_t launch_seal(sbc_graph* g, int n);
 cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq);
+int group_variant_count();
+int group_workers_per_sm(int v);
+// Append, classify + update, and seal (the steps selected) for the counts[s]
+// insertions staged in each member s's graph, on the group's stream.
+enum GroupSteps : unsigned { GROUP_APPEND = 1, GROUP_UPDATE = 2, GROUP_SEAL = 4, GROUP_ALL = 7 };
+cudaError_t launch_group_update(sbc_group* G, const int* counts, unsigned steps);
 }  // namespace sbc

@@ -43,6 +43,23 @@ struct DevGraph {
     const int32_t* seq;
 };
 
+// One forest as an update launch sees it: its graph, its root-major state and
+// the insertion batch staged for it (endpoints and append codes).
+struct ForestSlot {
+    DevGraph G;
+    const int64_t* roots;
+    int32_t* dist;
+    uint8_t* dist8;
+    int64_t* sigma;
+    double* delta;
+    double* bc;
+    const int32_t* ins_u;
+    const int32_t* ins_v;
+    const int32_t* ins_ok;
+    int nins;
+    int nk;
+};
+
 struct Scratch {
     int32_t* st;
     int64_t* dp;

@@ -35,24 +35,13 @@
 #include <climits>
 #include "sbc_host.h"
 #include "sbc_internal.cuh"
+#include "sbc_update_job.cuh"
 
 namespace sbc {
 
 struct UpdateArgs {
-    DevGraph G;
-    int64_t nv;
-    int nk;
-    const int64_t* roots;
-    int32_t* dist;
-    uint8_t* dist8;
-    int64_t* sigma;
-    double* delta;
-    double* bc;
+    ForestSlot f;
     ScratchBase scr;
-    int nins;
-    const int32_t* ins_u;
-    const int32_t* ins_v;
-    const int32_t* ins_ok;
     int all_visible;
     const int* worklist;
     const int* nwork;
@@ -60,384 +49,12 @@ struct UpdateArgs {
     unsigned long long* counters;  // vertices, edges, case1, case2, scanned
 };
 
-template <int NT>
-struct UpdSmem {
-    LbSmem<NT> lb;
-    int64_t dp[NT];
-    double wn[NT];
-    double wd[NT];
-    int fl[NT];
-    long long part[3 * (NT / 32) + 3];
-    int item, qt, at, st;
-    int nscan, nprobe;  // level-2 vertices whose parents are found by scan / by probe
-};
-
-// A level-2 vertex looks its parents up by binary search (one probe per root
-// neighbour) instead of scanning its adjacency when its degree exceeds this
-// many times the root's degree; a probe is costed as this many scanned slots.
-constexpr int kProbeRatio = 32;
-
-template <int NT>
-__device__ __forceinline__ void run_job(const UpdateArgs& A, UpdSmem<NT>& sm, const Scratch& W, int r,
-                                        int a, int b, bool moving, int g)
-{
-    const int64_t nv = A.nv;
-    int32_t* D = A.dist + (size_t)r * nv;
-    uint8_t* D8 = A.dist8 + (size_t)r * nv;
-    int64_t* S = A.sigma + (size_t)r * nv;
-    double* Dl = A.delta + (size_t)r * nv;
-    const int root = (int)A.roots[r];
-    const int Lb = D[a] + 1;  // new level of b; equals D[b] when |d| == 1
-
-    if (threadIdx.x == 0) {
-        W.st[b] = 1;
-        W.dp[b] = S[a];
-        W.qd[0] = b;
-        W.lvl[0] = 0;
-        W.lvl[1] = 1;
-        sm.qt = 1;
-        sm.at = 0;
-        sm.st = 0;
-        sm.nscan = 0;
-        sm.nprobe = 0;
-    }
-    __syncthreads();
-
-    // ---------------- descent ----------------
-    int step = 0, lo = 0, hi = 1;
-    while (lo < hi) {
-        const int L = Lb + step;
-        const int tag = step + 2;
-        lb_walk<NT>(
-            A.G, g, D, D8, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
-            [&](int j, int x, int d) { sm.dp[j] = W.dp[x]; },
-            [&](int j, int x, int k, int dk) {
-                if (moving ? (dk <= L) : (dk != L + 1)) return;
-                int s = W.st[k];
-                if (s == 0) {
-                    int old = atomicCAS(&W.st[k], 0, tag);
-                    if (old == 0) {
-                        int p = atomicAdd(&sm.qt, 1);
-                        W.qd[p] = k;
-                        s = tag;
-                    } else {
-                        s = old;
-                    }
-                }
-                if ((s & SBC_STEP_MASK) != tag) return;
-                atomic_add_i64(&W.dp[k], sm.dp[j]);
-            },
-            NoPost());
-        lo = hi;
-        hi = sm.qt;
-        ++step;
-        if (threadIdx.x == 0) W.lvl[step + 1] = hi;
-    }
-    const int ndown = hi;
-    const int nsteps = step;
-
-    // ---------------- re-level (|d| > 1) ----------------
-    if (moving) {
-        for (int i = threadIdx.x; i < ndown; i += NT) {
-            const int k = W.qd[i];
-            const int s = W.st[k];
-            const int nl = Lb + (s & SBC_STEP_MASK) - 1;
-            if (D[k] != nl) {
-                D[k] = nl;
-                D8[k] = enc_d8(nl);
-                W.st[k] = s | SBC_MOVED;
-            }
-        }
-    }
-    __syncthreads();
-
-    // ---------------- ascent ----------------
-    // A parent k's delta gains, per child x, sigma_k * (newdelta_x+1)/newsigma_x,
-    // and loses sigma_k * (olddelta_x+1)/oldsigma_x when k is not in the descent
-    // (k's sigma is then unchanged) -- except over the inserted edge (a, b),
-    // which had no old contribution.  acc[k] therefore sums the unscaled child
-    // weights wn = (newdelta+1)/newsigma or wd = wn - (olddelta+1)/oldsigma, and
-    // k's sigma multiplies the sum once, when k is committed: the walk over
-    // parent edges does no fp64 arithmetic (GB300's fp64 rate is a small
-    // fraction of its fp32 rate) and gathers no parent sigma.
-    int L = 0;
-    // Finalise vertex x of the level being walked: new sigma/delta committed in
-    // place, BC += newdelta - olddelta, and its child weights wn, wd returned.
-    auto commit = [&](int x, double& wn, double& wd) {
-        const int s = W.st[x];
-        const bool isDown = (s & SBC_STEP_MASK) != 0;
-        const bool mv = (s & SBC_MOVED) != 0;
-        const int64_t oS = S[x];
-        const double oD = Dl[x];
-        const double ac = W.acc[x];
-        const int64_t nS = isDown ? (mv ? W.dp[x] : oS + W.dp[x]) : oS;
-        const double nD = isDown ? (double)nS * ac : oD + (double)oS * ac;
-        wn = (nD + 1.0) / (double)nS;
-        wd = oS ? wn - (oD + 1.0) / (double)oS : wn;
-        if (x != root) atomicAdd(&A.bc[x], nD - oD);
-        S[x] = nS;
-        Dl[x] = nD;
-    };
-    auto prep = [&](int j, int x, int d) {
-        double wn, wd;
-        commit(x, wn, wd);
-        sm.wn[j] = wn;
-        sm.wd[j] = wd;
-        sm.fl[j] = ((W.st[x] & SBC_MOVED) ? 1 : 0) | (x == b ? 2 : 0);
-    };
-    // Child weights of an already committed vertex, kept in its acc/dp slots.
-    auto prep_loaded = [&](int j, int x, int d) {
-        sm.wn[j] = W.acc[x];
-        sm.wd[j] = __longlong_as_double((long long)W.dp[x]);
-        sm.fl[j] = ((W.st[x] & SBC_MOVED) ? 1 : 0) | (x == b ? 2 : 0);
-    };
-    auto parent_edge = [&](int j, int x, int k, int dk) -> bool {
-        if (dk != L - 1) return false;
-        const int sk = W.st[k];
-        const bool kDown = (sk & SBC_STEP_MASK) != 0;
-        if (!kDown && !(sk & SBC_ASC)) {
-            int old = atomicOr(&W.st[k], SBC_ASC);
-            if (!(old & SBC_ASC)) {
-                int p = atomicAdd(&sm.at, 1);
-                W.qa[p] = k;
-            }
-        }
-        const bool fresh = kDown || (k == a && (sm.fl[j] & 2));
-        atomicAdd(&W.acc[k], fresh ? sm.wn[j] : sm.wd[j]);
-        return true;
-    };
-
-    // Pull form for levels 1 and 2.  The parents of a level-1 vertex can only
-    // be the root, and those of a level-2 vertex only the root's neighbours, so
-    // instead of every walked vertex scanning its (often hub-sized) adjacency
-    // for parents, each candidate parent y can scan its own adjacency for
-    // walked children c (dist = L and touched) and sum the same child weights
-    // (wn[c] if y is in the descent or (y,c) = (a,b), else wd[c]).  The
-    // cheaper direction is chosen per level by scanned-slot count; results are
-    // the same either way.  Used only where no vertex of the level moved (no
-    // same-level ex-parent rule applies).
-    // The walked vertices of the level are marked in the worker's bitmap, so a
-    // candidate parent tests a neighbour with one (L2-resident) bit instead of
-    // gathering its distance and state.
-    auto pull_walk = [&](const int32_t* plist, int pn) {
-        lb_walk_sum<NT, false>(
-            A.G, g, D, D8, plist, pn, sm.lb, sm.wn, sm.fl,
-            [&](int j, int y, int d) {
-                const int sy = W.st[y];
-                sm.fl[j] = ((sy & SBC_STEP_MASK) ? 1 : 0) | (y == a ? 2 : 0);
-            },
-            [&](int j, int y, int c, int, double& v) -> bool {
-                if (!((W.bits[c >> 5] >> (c & 31)) & 1u)) return false;
-                const int fl = sm.fl[j];
-                const bool fresh = (fl & 1) || ((fl & 2) && c == b);
-                v = fresh ? W.acc[c] : __longlong_as_double((long long)W.dp[c]);
-                return true;
-            },
-            [&](int j, int y) {
-                const int fl = sm.fl[j];
-                if (!(fl & kSumHit)) return;
-                W.acc[y] += sm.wn[j];  // y's only contributions at this level come from this walk
-                if (!(fl & 1)) {
-                    int old = atomicOr(&W.st[y], SBC_ASC);
-                    if (!(old & SBC_ASC)) {
-                        int p = atomicAdd(&sm.at, 1);
-                        W.qa[p] = y;
-                    }
-                }
-            });
-    };
-    long long pull2_cost = -1;  // scanned slots of a level-2 pull (root's neighbours), computed once
-
-    // Level-2 parents of each listed (committed) vertex x: every root
-    // neighbour y (all at level 1) is looked up in x's sorted adjacency; a hit
-    // is a parent, which receives x's child weight (wn[x] if y is in the
-    // descent or (y,x) = (a,b), else wd[x]) and is claimed.  Warp per x, lanes
-    // over y.
-    auto probe_parents = [&](const int32_t* list, int n, int64_t rrow, int rdeg) {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        unsigned cost = 0;
-        for (int i = warp; i < n; i += NT / 32) {
-            const int x = list[i];
-            const int64_t rx = A.G.row[x];
-            const int vx = vis_deg(A.G, x, rx, g);
-            const double wn = W.acc[x];
-            const double wd = __longlong_as_double((long long)W.dp[x]);
-            for (int t = lane; t < rdeg; t += 32) {
-                const int y = A.G.col[rrow + t];
-                if (!has_edge(A.G, x, rx, vx, y, cost)) continue;
-                const int sy = W.st[y];
-                const bool yDown = (sy & SBC_STEP_MASK) != 0;
-                if (!yDown && !(sy & SBC_ASC)) {
-                    int old = atomicOr(&W.st[y], SBC_ASC);
-                    if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = y;
-                }
-                atomicAdd(&W.acc[y], (yDown || (y == a && x == b)) ? wn : wd);
-            }
-        }
-        if (cost) atomicAdd(&sm.lb.scanned_e, (unsigned long long)cost);
-        __syncthreads();
-    };
-
-    int ua_lo = 0, ua_hi = 0;
-    const int Lmax = Lb + nsteps - 1;
-    for (L = Lmax; L >= 0; --L) {
-        const int ds = L - Lb;
-        const int32_t* dlist = nullptr;
-        int dn = 0;
-        if (ds >= 0) {
-            dlist = W.qd + W.lvl[ds];
-            dn = W.lvl[ds + 1] - W.lvl[ds];
-        }
-        const int next_lo = sm.at;
-        const bool pull_ok = L >= 1 && L <= 2 && (!moving || L < Lb);
-        if (L == 0) {
-            // The root alone (if reached): no parents, committing is all.
-            if (threadIdx.x == 0 && dn + ua_hi - ua_lo > 0) {
-                const int x = dn ? dlist[0] : W.qa[ua_lo];
-                double wn, wd;
-                commit(x, wn, wd);
-                sm.lb.walked_v += 1;
-                sm.lb.walked_e += (unsigned)vis_deg(A.G, x, A.G.row[x], g);
-            }
-            __syncthreads();
-        } else if (pull_ok) {
-            // Commit every vertex x of the level and keep its push weights in
-            // its acc/dp slots; count it as traversed (reference counters).
-            //   L == 1  the only parent is the root (sigma 1): each x's
-            //           contribution is summed straight into the root, no scan.
-            //   L == 2  parents are N(x) ∩ N(root).  Per vertex, either scan
-            //           N(x) for distance-1 neighbours (push), or, when N(x) is
-            //           much longer than N(root), look each root neighbour up
-            //           in x's sorted adjacency (probe); or, for the whole
-            //           level, let the root's neighbours pull (bitmap test).
-            //           The cheapest plan by scanned slots is taken.
-            const int na_ = ua_hi - ua_lo;
-            const int64_t rrow = A.G.row[root];
-            const int rdeg = vis_deg(A.G, root, rrow, g);
-            const bool rootDown = (W.st[root] & SBC_STEP_MASK) != 0;
-            long long push_cost = 0, mixed_cost = 0;
-            double root_sum = 0.0;
-            const int qbase = sm.st;  // free tail of the same-level queue holds the two lists
-            for (int i = threadIdx.x; i < dn + na_; i += NT) {
-                const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
-                double wn, wd;
-                commit(x, wn, wd);
-                W.acc[x] = wn;
-                W.dp[x] = (int64_t)__double_as_longlong(wd);
-                const int dx = vis_deg(A.G, x, A.G.row[x], g);
-                push_cost += dx;
-                if (L == 1) {
-                    root_sum += (rootDown || (root == a && x == b)) ? wn : wd;
-                } else if (L == 2) {
-                    atomicOr(&W.bits[x >> 5], 1u << (x & 31));
-                    if ((long long)dx > (long long)kProbeRatio * rdeg) {
-                        W.qs[nv - 1 - atomicAdd(&sm.nprobe, 1)] = x;
-                        mixed_cost += (long long)kProbeRatio * rdeg;
-                    } else {
-                        W.qs[qbase + atomicAdd(&sm.nscan, 1)] = x;
-                        mixed_cost += dx;
-                    }
-                }
-            }
-            block_sum3<NT>(push_cost, mixed_cost, root_sum, sm.part);
-            if (threadIdx.x == 0) {
-                sm.lb.walked_v += (unsigned)(dn + na_);
-                sm.lb.walked_e += (unsigned long long)push_cost;
-            }
-            if (L == 1) {
-                if (threadIdx.x == 0 && dn + na_ > 0) {
-                    W.acc[root] += root_sum;
-                    if (!rootDown) {
-                        int old = atomicOr(&W.st[root], SBC_ASC);
-                        if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = root;
-                    }
-                }
-                __syncthreads();
-            } else if (L == 2 && dn + na_ > 0) {
-                if (pull2_cost < 0) {
-                    long long c = 0;
-                    for (int i = threadIdx.x; i < rdeg; i += NT) {
-                        const int y = A.G.col[rrow + i];
-                        c += vis_deg(A.G, y, A.G.row[y], g);
-                    }
-                    pull2_cost = block_sum<NT>(c, sm.part);
-                }
-                if (pull2_cost < mixed_cost) {
-                    pull_walk(A.G.col + rrow, rdeg);
-                } else {
-                    const int nscan = sm.nscan, nprobe = sm.nprobe;
-                    lb_walk<NT, false>(A.G, g, D, D8, W.qs + qbase, nscan, nullptr, 0, sm.lb, prep_loaded,
-                                       [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
-                    probe_parents(W.qs + nv - nprobe, nprobe, rrow, rdeg);
-                }
-                for (int i = threadIdx.x; i < dn + na_; i += NT) {
-                    const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
-                    W.bits[x >> 5] = 0u;  // words hold only this level's marks
-                }
-                __syncthreads();
-            }
-        } else if (!moving) {
-            lb_walk<NT>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,
-                        [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
-        } else {
-            const int same_lo = sm.st;
-            lb_walk<NT>(
-                A.G, g, D, D8, dlist, dn, nullptr, 0, sm.lb, prep,
-                [&](int j, int x, int k, int dk) {
-                    if (parent_edge(j, x, k, dk)) return;
-                    if (!(sm.fl[j] & 1) || dk != L) return;
-                    // k kept its level and lost the moved vertex x as a child
-                    const int sk = W.st[k];
-                    if (sk & SBC_STEP_MASK) return;
-                    if (!(sk & SBC_ASC)) {
-                        int old = atomicOr(&W.st[k], SBC_ASC);
-                        if (!(old & SBC_ASC)) {
-                            int p = atomicAdd(&sm.st, 1);
-                            W.qs[p] = k;
-                        }
-                    }
-                    atomicAdd(&W.acc[k], sm.wd[j] - sm.wn[j]);
-                },
-                NoPost());
-            const int same_hi = sm.st;
-            lb_walk<NT>(A.G, g, D, D8, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
-                        prep, [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
-        }
-        ua_lo = next_lo;
-        ua_hi = sm.at;
-        if (L <= Lb && ua_lo == ua_hi) break;
-    }
-
-    // ---------------- reset touched scratch ----------------
-    const int na = sm.at, ns = sm.st;
-    for (int i = threadIdx.x; i < ndown; i += NT) {
-        const int k = W.qd[i];
-        W.st[k] = 0;
-        W.dp[k] = 0;
-        W.acc[k] = 0.0;
-    }
-    for (int i = threadIdx.x; i < na; i += NT) {
-        const int k = W.qa[i];
-        W.st[k] = 0;
-        W.dp[k] = 0;  // may hold a push weight (pull-form levels)
-        W.acc[k] = 0.0;
-    }
-    for (int i = threadIdx.x; i < ns; i += NT) {
-        const int k = W.qs[i];
-        W.st[k] = 0;
-        W.acc[k] = 0.0;
-    }
-    __syncthreads();
-}
-
 template <int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) k_update(UpdateArgs A)
+__global__ void __launch_bounds__(NT, MINB) k_update(const __grid_constant__ UpdateArgs A)
 {
     __shared__ UpdSmem<NT> sm;
-    const int64_t nv = A.nv;
-    const Scratch W = A.scr.of(blockIdx.x, nv);
+    const Scratch W = A.scr.of(blockIdx.x, A.f.G.nv);
     const int nwork = *A.nwork;
-    const int g_all = INT_MAX;
     unsigned long long c1 = 0, c2 = 0;
     if (threadIdx.x == 0) sm.lb.walked_v = sm.lb.walked_e = sm.lb.scanned_e = 0;
 
@@ -447,31 +64,9 @@ __global__ void __launch_bounds__(NT, MINB) k_update(UpdateArgs A)
         const int item = sm.item;
         __syncthreads();
         if (item >= nwork) break;
-        const int r = A.worklist[item];
-        const int32_t* D = A.dist + (size_t)r * nv;
-        for (int i = 0; i < A.nins; ++i) {
-            if (A.ins_ok[i] <= 0) continue;
-            const int u = A.ins_u[i], v = A.ins_v[i];
-            const int du = D[u], dv = D[v];
-            if (du == dv) continue;  // same level, or both unreachable
-            const int b = du > dv ? u : v;
-            const int a = du > dv ? v : u;
-            const int db = du > dv ? du : dv, da = du > dv ? dv : du;
-            const bool moving = (db == SBC_INF) || (db - da > 1);
-            if (threadIdx.x == 0) {
-                if (moving) c2++;
-                else c1++;
-            }
-            run_job<NT>(A, sm, W, r, a, b, moving, A.all_visible ? g_all : i);
-        }
+        process_root<NT>(A.f, sm, W, A.worklist[item], A.all_visible != 0, c1, c2);
     }
-    if (threadIdx.x == 0) {
-        atomicAdd(&A.counters[0], sm.lb.walked_v);
-        atomicAdd(&A.counters[1], sm.lb.walked_e);
-        atomicAdd(&A.counters[2], c1);
-        atomicAdd(&A.counters[3], c2);
-        atomicAdd(&A.counters[4], sm.lb.scanned_e);
-    }
+    flush_counters<NT>(sm, A.counters, c1, c2);
 }
 
 __global__ void k_classify(const int32_t* __restrict__ dist, int64_t nv, int nk, int nins,
@@ -557,20 +152,8 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     f->prof_end(PROF_CLASSIFY);
     if ((e = cudaGetLastError())) return e;
     UpdateArgs A;
-    A.G = g->dev();
-    A.nv = f->nv;
-    A.nk = (int)f->nk;
-    A.roots = f->d_roots;
-    A.dist = f->d_dist;
-    A.dist8 = f->d_dist8;
-    A.sigma = f->d_sigma;
-    A.delta = f->d_delta;
-    A.bc = f->d_bc;
+    A.f = forest_slot(f, n);
     A.scr = f->scratch();
-    A.nins = n;
-    A.ins_u = iu;
-    A.ins_v = iv;
-    A.ins_ok = ok;
     A.all_visible = all_visible ? 1 : 0;
     A.worklist = f->d_worklist;
     A.nwork = f->d_nwork;

@@ -313,6 +313,23 @@ def insert_edges(g: Graph, ins: np.ndarray) -> Graph:
 # Named workloads (sizes as stated for each benchmark configuration).
 # --------------------------------------------------------------------------
 
+def rmat_group(count: int = 64, scale_lo: int = 10, scale_hi: int = 16, edge_factor: int = 8, seed0: int = 100,
+               k_max: int = 128, insertions: int = 512):
+    """Independent R-MAT graphs for multi-forest batches: graph i has a scale
+    drawn uniformly from [scale_lo, scale_hi] (one generator seeded with
+    seed0), edge factor `edge_factor`, seed seed0 + i, K = min(|V|, k_max)
+    uniform roots and `insertions` R-MAT-drawn new edges.
+    Returns a list of (graph, roots, insertions, scale)."""
+    scales = np.random.default_rng(seed0).integers(scale_lo, scale_hi + 1, size=count)
+    out = []
+    for i, sc in enumerate(scales):
+        sc = int(sc)
+        g = rmat(sc, edge_factor, seed=seed0 + i)
+        roots = pick_roots(g.nv, min(g.nv, k_max), seed=seed0 + i)
+        out.append((g, roots, rmat_insertions(g, sc, insertions, seed=seed0 + i), sc))
+    return out
+
+
 def workload(name: str, small: bool = False):
     """(graph, roots, insertions) for a named workload.
 

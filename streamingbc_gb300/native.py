@@ -102,6 +102,13 @@ def load(path: str = LIB_PATH):
         "sbc_forest_variant": (C.c_int, [_vp, C.POINTER(C.c_int)]),
         "sbc_forest_autotune": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.c_int, C.POINTER(C.c_int), _f64p,
                                           C.c_int]),
+        "sbc_group_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp), C.c_int]),
+        "sbc_group_destroy": (C.c_int, [_vp]),
+        "sbc_group_info": (C.c_int, [_vp, C.POINTER(C.c_int), _i64p, _i64p, C.POINTER(C.c_int)]),
+        "sbc_group_set_variant": (C.c_int, [_vp, C.c_int]),
+        "sbc_group_insert_batch": (C.c_int, [_vp, _i64p, _i64p, _i64p, _f64p]),
+        "sbc_group_autotune": (C.c_int, [_vp, _i64p, _i64p, _i64p, C.c_int, C.POINTER(C.c_int), _f64p, C.c_int]),
+        "sbc_group_read_counters": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
         "sbc_update_inserted": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
         "sbc_sync": (C.c_int, [_vp]),
         "sbc_read_counters": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p, _i64p]),
@@ -206,6 +213,7 @@ class DeviceForest:
         self.nv = graph.nv
         self.nk = int(self.roots.size)
         graph._forests.add(self)
+        self._groups = weakref.WeakSet()
 
     def info(self) -> dict:
         v = [C.c_int64() for _ in range(4)]
@@ -324,6 +332,8 @@ class DeviceForest:
         return ms.value
 
     def close(self):
+        for grp in list(getattr(self, "_groups", ())):
+            grp.close()  # a live group holds this forest
         if getattr(self, "h", None):
             self.lib.sbc_forest_destroy(self.h)
             self.h = None
@@ -333,3 +343,73 @@ class DeviceForest:
             self.close()
         except Exception:
             pass
+
+
+class DeviceGroup:
+    """sbc_group: up to 64 forests over different graphs, updated by one
+    append, one classify and one persistent update launch per batch."""
+
+    def __init__(self, forests, variant: int = -1):
+        self.lib = load()
+        self.forests = list(forests)
+        arr = (_vp * len(self.forests))(*[f.h for f in self.forests])
+        h = _vp()
+        _check(self.lib.sbc_group_create(C.byref(h), len(self.forests), arr, int(variant)))
+        self.h = h
+        for f in self.forests:
+            f._groups.add(self)
+
+    @staticmethod
+    def _flatten(batches):
+        parts = [np.asarray(b, dtype=np.int64).reshape(-1, 2) for b in batches]
+        counts = np.array([len(p) for p in parts], dtype=np.int64)
+        cat = np.concatenate(parts) if len(parts) else np.zeros((0, 2), np.int64)
+        return counts, np.ascontiguousarray(cat[:, 0]), np.ascontiguousarray(cat[:, 1])
+
+    def insert(self, batches) -> float:
+        """Apply batches[i] (pairs) to forests[i], all in one launch sequence;
+        returns the device time of that sequence in ms."""
+        counts, u, v = self._flatten(batches)
+        if len(counts) != len(self.forests):
+            raise ValueError("one batch per member forest")
+        ms = C.c_double(0.0)
+        _check(self.lib.sbc_group_insert_batch(self.h, p64(counts), p64(u), p64(v), C.byref(ms)))
+        return ms.value
+
+    def autotune(self, batches, reps: int = 2):
+        counts, u, v = self._flatten(batches)
+        if len(counts) != len(self.forests):
+            raise ValueError("one batch per member forest")
+        n = C.c_int(0)
+        _check(self.lib.sbc_update_variant_count(C.byref(n)))
+        ms = np.full(n.value, -1.0)
+        chosen = C.c_int(-1)
+        _check(self.lib.sbc_group_autotune(self.h, p64(counts), p64(u), p64(v), int(reps), C.byref(chosen),
+                                           ms.ctypes.data_as(_f64p), n.value))
+        return chosen.value, ms
+
+    def set_variant(self, variant: int):
+        _check(self.lib.sbc_group_set_variant(self.h, int(variant)))
+
+    def info(self) -> dict:
+        n, var = C.c_int(0), C.c_int(0)
+        w, b = C.c_int64(0), C.c_int64(0)
+        _check(self.lib.sbc_group_info(self.h, C.byref(n), C.byref(w), C.byref(b), C.byref(var)))
+        return {"forests": n.value, "workers": w.value, "bytes": b.value, "variant": var.value}
+
+    def counters(self) -> dict:
+        v = [C.c_int64() for _ in range(5)]
+        _check(self.lib.sbc_group_read_counters(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("vertices", "edges", "case1", "case2", "scanned"), [x.value for x in v]))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sbc_group_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
