@@ -57,6 +57,12 @@ def parse():
     p.add_argument("--variant", type=int, default=-1,
                    help="update-kernel launch shape (-1 = autotuned on the first warm-up batch)")
     p.add_argument("--workers", type=int, default=0, help="persistent workers (0 = automatic)")
+    p.add_argument("--train-insertions", type=int, default=-1,
+                   help="cost model: insertions whose per-job costs are logged for training "
+                        "(-1 = 16384 on rmat20, else 0 = static schedule)")
+    p.add_argument("--train-epochs", type=int, default=4)
+    p.add_argument("--compare-batches", type=int, default=8,
+                   help="batches timed under both schedules after training")
     p.add_argument("--roots", type=int, default=0,
                    help="use only the first N roots of the workload (profiling captures; 0 = all)")
     return p.parse_args()
@@ -419,19 +425,55 @@ def run_ours(args):
     n_dev = (args.warmup + 2 * args.steps) * B
     n_e2e = 0 if args.no_e2e else (1 + args.steps) * B
     n_plain = args.plain
+    # cost model: log per-job costs over the first `train` insertions, train,
+    # then time `compare` batches under both schedules (paired, on copies)
+    train = args.train_insertions if args.train_insertions >= 0 else (16384 if args.workload == "rmat20" else 0)
+    n_cmp = args.compare_batches * B if train > 0 else 0
+    n_pre = train + n_cmp
     t0 = time.time()
-    g, roots, ins = load_workload(args.workload, n_dev + n_e2e + n_plain)
+    g, roots, ins_all = load_workload(args.workload, n_pre + n_dev + n_e2e + n_plain)
     if args.roots:
         roots = roots[:args.roots]
     gen_s = time.time() - t0
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
     f = native.DeviceForest(dg, roots, workers=args.workers, variant=args.variant)
-    dg.reserve(ins)  # slack for every insertion of the run, planned before timing
+    dg.reserve(ins_all)  # slack for every insertion of the run, planned before timing
 
     t0 = time.time()
     f.static_init()
     static_s = time.time() - t0
     f.counters()
+
+    model_info = None
+    if train > 0:
+        K0 = len(roots)
+        pre = torch.tensor(ins_all[:train], dtype=torch.int32, device="cuda")
+        p_u, p_v = pre[:, 0].contiguous(), pre[:, 1].contiguous()
+        f.cost_log_start(min(train * K0, 1 << 26))
+        t0 = time.time()
+        for s in range(0, train - B + 1, B):
+            f.insert_device(B, p_u[s:].data_ptr(), p_v[s:].data_ptr())
+        f.sync()
+        log_s = time.time() - t0
+        samples = f.cost_log_stop()
+        tstats = f.train_cost_model(epochs=args.train_epochs, batch=4096, lr=2e-3, val_frac=0.1, seed=1)
+        f.set_schedule(native.DeviceForest.SCHED_MODEL)
+        ms_s = ms_m = 0.0
+        for s in range(train, train + n_cmp, B):
+            a, b_ = f.compare_schedules(ins_all[s:s + B], reps=1)
+            ms_s += a
+            ms_m += b_
+        f.counters()
+        model_info = {"train_insertions": train, "logged_samples": samples, "logging_s": log_s,
+                      "train": {k: tstats[k] for k in ("train_samples", "val_samples", "epochs", "steps",
+                                                      "train_ms", "val_mae", "val_rmse", "val_mae_mean")},
+                      "target": "log(1 + touched vertices) per (insertion, root) job",
+                      "schedule_compare": {"batches": args.compare_batches, "static_ms": ms_s, "model_ms": ms_m,
+                                           "static_over_model": ms_s / ms_m if ms_m > 0 else None,
+                                           "note": "same batches, each timed under both schedules on copies of "
+                                                   "the state (classify/ordering + update)"},
+                      "schedule": "model"}
+    ins = ins_all[n_pre:]
 
     # ---------------- device-resident batches (value) ----------------
     d_ins = torch.tensor(ins[:n_dev], dtype=torch.int32, device="cuda")
@@ -546,7 +588,7 @@ def run_ours(args):
     if not args.no_cpu and rank == 0:
         threads = os.cpu_count() or 1
         nr = args.cpu_roots or min(len(roots), 2 * threads)
-        cpu = cpu_sample(g, roots, ins, nr, args.cpu_insertions, threads)
+        cpu = cpu_sample(g, roots, ins_all, nr, args.cpu_insertions, threads)
 
     info = f.info()
     if rank == 0:
@@ -572,7 +614,10 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clocks,
-            "gpu_launches": 6 * args.steps,  # set_src, stage, append, classify, update, seal per batch
+            # set_src, stage, append, classify, update, seal per batch; under the
+            # model schedule classify becomes features + 3 ordering kernels
+            "gpu_launches": (9 if model_info else 6) * args.steps,
+            "cost_model": model_info,
             "plain_gpu": plain,
             "latency_ms": {"batch_p50": batch_ms, "wall_ms_timed": wall_ms,
                            "per_insertion_in_batch": batch_ms},

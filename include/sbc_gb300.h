@@ -165,6 +165,60 @@ int sbc_forest_autotune(sbc_forest *f, int64_t n, const int64_t *u, const int64_
  * Synchronous; stats may be NULL. */
 int sbc_update_inserted(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, sbc_batch_stats *stats);
 
+/* ---- learned cost model and batch schedule --------------------------------
+ * The reference orders roots statically under BALANCE (qsort by
+ * 2*edgesBelow + edgesAbove, src/streamingbc.c:171-188).  Here an FP32 MLP
+ * (8 features -> 64 -> 64 -> 1, ReLU; sbc_cost_model_size gives the parameter
+ * count) predicts log(1 + touched vertices) of each (insertion, root) job
+ * from features taken at batch start: d(r,a), d(r,b) for the shallower and
+ * deeper endpoint (64 = unreachable), their level difference, log1p of
+ * deg(a), deg(b), sigma(r,a), sigma(r,b), and log1p of the number of vertices
+ * at level d(r,a)+1 of r's tree.  Under SBC_SCHED_MODEL each batch's active
+ * roots are queued longest predicted batch cost first; SBC_SCHED_STATIC
+ * (the default and the fallback) keeps the classify order.  Results never
+ * depend on the schedule.  Training data are logged by the update kernel:
+ * sbc_cost_log_start makes every later batch append (features, log1p of the
+ * job's touched vertices) of each job it runs, up to `capacity` samples. */
+#define SBC_SCHED_STATIC 0
+#define SBC_SCHED_MODEL 1
+typedef struct {
+    int64_t samples, train_samples, val_samples, steps;
+    int epochs;
+    double train_ms;      /* device time of the training kernels */
+    double val_mae;       /* held-out mean |error| in log(1 + touched) */
+    double val_rmse;
+    double val_mae_mean;  /* held-out mean |error| of predicting the training mean */
+} sbc_model_stats;
+int sbc_cost_model_size(int *n_params, int *n_features);
+int sbc_cost_log_start(sbc_forest *f, int64_t capacity);
+int sbc_cost_log_stop(sbc_forest *f, int64_t *samples);
+/* Logged samples [first, first+count): x[count][n_features], y[count]. */
+int sbc_cost_log_read(sbc_forest *f, int64_t first, int64_t count, float *x, float *y);
+/* Adam on the mean squared error over the first (1 - val_frac) of the logged
+ * samples, `epochs` passes in minibatches of `batch` (a multiple of 128);
+ * the rest is held out for the reported error.  Synchronous. */
+int sbc_cost_model_train(sbc_forest *f, int epochs, int batch, double lr, double val_frac, uint64_t seed,
+                         sbc_model_stats *stats);
+int sbc_set_schedule(sbc_forest *f, int schedule);
+/* Insert the batch (u[i], v[i]) like sbc_insert_batch, after timing its
+ * update (classify or features + ordering, and the update kernel) under each
+ * schedule on fresh copies of the state (reps runs each, fastest kept).
+ * Needs a trained model; the forest's own schedule is unchanged. */
+int sbc_forest_compare_schedules(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, int reps,
+                                 double *ms_static, double *ms_model);
+/* Read (get) and/or replace (set) the n_params parameters (set marks the
+ * model trained).  Layout: W1[8][64], b1[64], W2[64][64], b2[64], w3[64], b3,
+ * feature means[8], inverse feature standard deviations[8]. */
+int sbc_cost_model_params(sbc_forest *f, float *get, const float *set);
+/* Model outputs for n feature rows (host arrays). */
+int sbc_cost_model_predict(sbc_forest *f, int64_t n, const float *x, float *out);
+/* Gradient of the mean squared error over n <= 65536 samples at the current
+ * parameters (n_params - 16 trained entries), and the predictions. */
+int sbc_cost_model_grad(sbc_forest *f, int64_t n, const float *x, const float *y, float *grad, float *pred);
+/* Per-root level histograms rows [r0, r0+nr): 64 counts each (the last
+ * counts level 63 and deeper). */
+int sbc_get_level_hist(sbc_forest *f, int64_t r0, int64_t nr, int32_t *out);
+
 /* ---- groups: many forests updated by one launch per batch --------------
  * The reference updates one forest per insertEdgeStreamingBC call
  * (src/streamingbc.c:88-226); a group applies one batch to each of up to 64

@@ -1,10 +1,12 @@
 // C-ABI of libsbc_gb300.so: sbc_* entry points (include/sbc_gb300.h), the
 // drop-in streamingbc.h surface of the reference and the STINGER shim.
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <random>
 #include <unordered_map>
 #include <vector>
 
@@ -292,6 +294,65 @@ void drop_captured(sbc_forest* f)
     f->captured.clear();
 }
 
+void free_model(sbc_forest* f)
+{
+    CostModel* M = f->model;
+    if (!M) return;
+    dev_free(M->d_params);
+    dev_free(M->d_m);
+    dev_free(M->d_v);
+    dev_free(M->d_grad);
+    dev_free(M->d_x);
+    dev_free(M->d_y);
+    dev_free(M->d_n);
+    dev_free(M->d_sums);
+    dev_free(M->d_feat);
+    dev_free(M->d_cost_log);
+    dev_free(M->d_root_cost);
+    dev_free(M->d_buckets);
+    delete M;
+    f->model = nullptr;
+}
+
+// The cost model's parameters, optimiser state and accumulators, on first use.
+int ensure_model(sbc_forest* f)
+{
+    if (f->model) return SBC_OK;
+    CostModel* M = new CostModel();
+    f->model = M;
+    cudaError_t e;
+    if ((e = dev_alloc(&M->d_params, sbc::kModelParams)) || (e = dev_alloc(&M->d_m, sbc::kTrainParams)) ||
+        (e = dev_alloc(&M->d_v, sbc::kTrainParams)) || (e = dev_alloc(&M->d_grad, sbc::kTrainParams)) ||
+        (e = dev_alloc(&M->d_n, 1)) || (e = dev_alloc(&M->d_sums, 32)) || (e = dev_alloc(&M->d_root_cost, f->nk)) ||
+        (e = dev_alloc(&M->d_buckets, sbc::kCostBuckets)) ||
+        (e = cudaMemsetAsync(M->d_params, 0, sizeof(float) * sbc::kModelParams, f->g->stream)) ||
+        (e = cudaMemsetAsync(M->d_grad, 0, sizeof(float) * sbc::kTrainParams, f->g->stream)) ||
+        (e = cudaMemsetAsync(M->d_n, 0, sizeof(unsigned long long), f->g->stream))) {
+        free_model(f);
+        return cuda_fail(e, "cost model allocation");
+    }
+    return SBC_OK;
+}
+
+// Per-batch log buffers (features and costs of every (root, insertion) pair)
+// for batches of up to n insertions.  Captured batch graphs hold the old
+// buffers, so they are dropped when the buffers move.
+int ensure_model_batch(sbc_forest* f, int64_t n)
+{
+    CostModel* M = f->model;
+    if (!M || !M->logging || M->log_ins >= n) return SBC_OK;
+    dev_free(M->d_feat);
+    dev_free(M->d_cost_log);
+    M->log_ins = 0;
+    cudaError_t e;
+    const size_t pairs = (size_t)f->nk * (size_t)n;
+    if ((e = dev_alloc(&M->d_feat, pairs * sbc::kIn)) || (e = dev_alloc(&M->d_cost_log, pairs)))
+        return cuda_fail(e, "cost log buffers");
+    M->log_ins = n;
+    drop_captured(f);
+    return SBC_OK;
+}
+
 size_t scratch_per_worker(int64_t nv) { return WorkerScratch::per_worker(nv); }
 
 // Worker count of launch shape `variant`: one per CTA the update kernel keeps
@@ -341,13 +402,15 @@ struct TrialState {
     int64_t* sigma = nullptr;
     double* delta = nullptr;
     double* bc = nullptr;
+    int32_t* hist = nullptr;
     cudaError_t alloc(const sbc_forest* f, int64_t rows)
     {
         nk = rows;
         const size_t cells = (size_t)rows * (size_t)f->nv;
         cudaError_t e;
         if ((e = dev_alloc(&dist, cells)) || (e = dev_alloc(&dist8, cells)) || (e = dev_alloc(&sigma, cells)) ||
-            (e = dev_alloc(&delta, cells)) || (e = dev_alloc(&bc, f->nv)))
+            (e = dev_alloc(&delta, cells)) || (e = dev_alloc(&bc, f->nv)) ||
+            (f->d_lvlhist && (e = dev_alloc(&hist, (size_t)rows * sbc::kHistLevels))))
             release();
         return e;
     }
@@ -358,6 +421,7 @@ struct TrialState {
         dev_free(sigma);
         dev_free(delta);
         dev_free(bc);
+        dev_free(hist);
     }
     cudaError_t copy_from(const sbc_forest* f, cudaStream_t s) const
     {
@@ -368,7 +432,8 @@ struct TrialState {
             (e = cudaMemcpyAsync(dist8, f->d_dist8, cells, d2d, s)) ||
             (e = cudaMemcpyAsync(sigma, f->d_sigma, sizeof(int64_t) * cells, d2d, s)) ||
             (e = cudaMemcpyAsync(delta, f->d_delta, sizeof(double) * cells, d2d, s)) ||
-            (e = cudaMemcpyAsync(bc, f->d_bc, sizeof(double) * f->nv, d2d, s)))
+            (e = cudaMemcpyAsync(bc, f->d_bc, sizeof(double) * f->nv, d2d, s)) ||
+            (hist && (e = cudaMemcpyAsync(hist, f->d_lvlhist, sizeof(int32_t) * (size_t)nk * sbc::kHistLevels, d2d, s))))
             return e;
         return cudaSuccess;
     }
@@ -379,6 +444,7 @@ struct TrialState {
         std::swap(f->d_sigma, sigma);
         std::swap(f->d_delta, delta);
         std::swap(f->d_bc, bc);
+        if (hist) std::swap(f->d_lvlhist, hist);
         std::swap(f->nk, nk);
     }
 };
@@ -704,7 +770,8 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     if ((e = dev_alloc(&f->d_roots, nk)) || (e = dev_alloc(&f->d_dist, cells)) || (e = dev_alloc(&f->d_dist8, cells)) ||
         (e = dev_alloc(&f->d_sigma, cells)) ||
         (e = dev_alloc(&f->d_delta, cells)) || (e = dev_alloc(&f->d_bc, f->nv)) || (e = dev_alloc(&f->d_worklist, nk)) ||
-        (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, SBC_NCOUNTERS))) {
+        (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, SBC_NCOUNTERS)) ||
+        (e = dev_alloc(&f->d_lvlhist, (size_t)nk * sbc::kHistLevels))) {
         sbc_forest_destroy(f);
         return cuda_fail(e, "sbc_forest_create state allocation");
     }
@@ -746,6 +813,8 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_worklist);
     dev_free(f->d_nwork);
     dev_free(f->d_counters);
+    dev_free(f->d_lvlhist);
+    free_model(f);
     free_scratch(f);
     f->prof_release();
     drop_captured(f);
@@ -771,6 +840,7 @@ int sbc_static_init(sbc_forest* f)
     if (!f) return fail(SBC_ERR_ARG, "sbc_static_init: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(sbc::launch_static(f));
+    CK(sbc::launch_level_hist(f));
     f->initialized = true;
     return SBC_OK;
 }
@@ -790,6 +860,7 @@ int sbc_insert_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* 
     int rc = plan_capacity(g, n, u, v, false);
     if (rc) return rc;
     if ((rc = stage_host(g, n, u, v, false))) return rc;
+    if ((rc = ensure_model_batch(f, g->ins_capacity))) return rc;
     // per-call statistics cover this call only
     if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
     f->prof_begin(sbc::PROF_BATCH);
@@ -814,6 +885,7 @@ int sbc_insert_batch_device(sbc_forest* f, int64_t n, const int32_t* d_u, const 
     if (use_device(g->device)) return SBC_ERR_CUDA;
     int rc = ensure_staging(g, n);
     if (rc) return rc;
+    if ((rc = ensure_model_batch(f, g->ins_capacity))) return rc;
     if (f->use_graphs && !f->prof) return replay_batch(f, (int)n, d_u, d_v);
     f->prof_begin(sbc::PROF_BATCH);
     CK(sbc::launch_set_src(g, d_u, d_v));
@@ -881,6 +953,9 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
     CK(cudaMemGetInfo(&free_b, &total_b));
     const int64_t nk_t = std::min<int64_t>(f->nk, (int64_t)((free_b / 2) / ((size_t)f->nv * 21)));
     if (nk_t < 1) return fail(SBC_ERR_CUDA, "sbc_forest_autotune: no memory for a trial copy of one root");
+    if ((rc = ensure_model_batch(f, g->ins_capacity))) return rc;
+    const bool logging = f->model && f->model->logging;
+    if (logging) f->model->logging = false;  // timing runs log nothing
     TrialState T;
     unsigned long long saved_counters[SBC_NCOUNTERS];
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -894,6 +969,7 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
         f->prof = prof;
+        if (logging) f->model->logging = true;
     };
     if ((e = T.alloc(f, nk_t)) || (e = cudaEventCreate(&e0)) || (e = cudaEventCreate(&e1)) ||
         (e = cudaMemcpyAsync(saved_counters, f->d_counters, sizeof saved_counters, cudaMemcpyDeviceToHost, g->stream)) ||
@@ -947,6 +1023,306 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
     CK(sbc::launch_seal(g, (int)n));
     if (chosen) *chosen = best;
     return check_graph_err(g);
+}
+
+// ------------------------------------------------------------------ cost model
+
+int sbc_cost_model_size(int* n_params, int* n_features)
+{
+    if (n_params) *n_params = sbc::kModelParams;
+    if (n_features) *n_features = sbc::kIn;
+    return SBC_OK;
+}
+
+int sbc_cost_log_start(sbc_forest* f, int64_t capacity)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_cost_log_start: the forest's graph was destroyed");
+    if (!f || capacity <= 0 || capacity >= ((int64_t)1 << 31))
+        return fail(SBC_ERR_ARG, "sbc_cost_log_start: bad arguments");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    int rc = ensure_model(f);
+    if (rc) return rc;
+    CostModel* M = f->model;
+    CK(cudaStreamSynchronize(f->g->stream));
+    if (capacity != M->capacity) {
+        dev_free(M->d_x);
+        dev_free(M->d_y);
+        M->capacity = 0;
+        cudaError_t e;
+        if ((e = dev_alloc(&M->d_x, (size_t)capacity * sbc::kIn)) || (e = dev_alloc(&M->d_y, (size_t)capacity)))
+            return cuda_fail(e, "cost log allocation");
+        M->capacity = capacity;
+        CK(cudaMemset(M->d_n, 0, sizeof(unsigned long long)));
+    }
+    M->logging = true;
+    drop_captured(f);
+    return ensure_model_batch(f, f->g->ins_capacity);
+}
+
+int sbc_cost_log_stop(sbc_forest* f, int64_t* samples)
+{
+    if (!f || !f->g) return fail(SBC_ERR_ARG, "sbc_cost_log_stop: null forest or graph");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaStreamSynchronize(f->g->stream));
+    if (f->model) {
+        f->model->logging = false;
+        drop_captured(f);
+    }
+    if (samples) {
+        unsigned long long n = 0;
+        if (f->model) CK(cudaMemcpy(&n, f->model->d_n, sizeof n, cudaMemcpyDeviceToHost));
+        *samples = f->model ? std::min<int64_t>((int64_t)n, f->model->capacity) : 0;
+    }
+    return SBC_OK;
+}
+
+int sbc_cost_log_read(sbc_forest* f, int64_t first, int64_t count, float* x, float* y)
+{
+    if (!f || !f->g || !f->model || first < 0 || count < 0 || first + count > f->model->capacity)
+        return fail(SBC_ERR_ARG, "sbc_cost_log_read: bad arguments");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaStreamSynchronize(f->g->stream));
+    if (x) CK(cudaMemcpy(x, f->model->d_x + first * sbc::kIn, sizeof(float) * count * sbc::kIn, cudaMemcpyDeviceToHost));
+    if (y) CK(cudaMemcpy(y, f->model->d_y + first, sizeof(float) * count, cudaMemcpyDeviceToHost));
+    return SBC_OK;
+}
+
+int sbc_cost_model_train(sbc_forest* f, int epochs, int batch, double lr, double val_frac, uint64_t seed,
+                         sbc_model_stats* st)
+{
+    if (!f || !f->g || !f->model || epochs < 1 || batch < 128 || batch % 128 || lr <= 0 || val_frac < 0 ||
+        val_frac >= 1)
+        return fail(SBC_ERR_ARG, "sbc_cost_model_train: bad arguments (log costs first; batch a multiple of 128)");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CostModel* M = f->model;
+    cudaStream_t s = f->g->stream;
+    CK(cudaStreamSynchronize(s));
+    unsigned long long logged = 0;
+    CK(cudaMemcpy(&logged, M->d_n, sizeof logged, cudaMemcpyDeviceToHost));
+    const int64_t n = std::min<int64_t>((int64_t)logged, M->capacity);
+    const int64_t nval = (int64_t)((double)n * val_frac);
+    const int64_t ntr = n - nval;
+    if (ntr < batch) return fail(SBC_ERR_STATE, "sbc_cost_model_train: %lld logged samples, too few", (long long)n);
+    // feature normalisation and the target mean from the training part
+    CK(sbc::launch_moments(f, ntr));
+    double sums[32];
+    CK(cudaMemcpyAsync(sums, M->d_sums, sizeof sums, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<float> P(sbc::kModelParams, 0.f);
+    std::mt19937_64 rng(seed);
+    auto uni = [&](float lim) { return (float)(((double)(rng() >> 11) / 9007199254740992.0) * 2.0 - 1.0) * lim; };
+    for (int i = 0; i < sbc::kIn * sbc::kH; ++i) P[sbc::OFF_W1 + i] = uni(std::sqrt(6.f / sbc::kIn));
+    for (int i = 0; i < sbc::kH * sbc::kH; ++i) P[sbc::OFF_W2 + i] = uni(std::sqrt(6.f / sbc::kH));
+    for (int i = 0; i < sbc::kH; ++i) P[sbc::OFF_W3 + i] = uni(std::sqrt(3.f / sbc::kH));
+    const float ymean = (float)(sums[2 * sbc::kIn] / (double)ntr);
+    P[sbc::OFF_B3] = ymean;
+    for (int k = 0; k < sbc::kIn; ++k) {
+        const double mu = sums[k] / (double)ntr;
+        const double var = sums[sbc::kIn + k] / (double)ntr - mu * mu;
+        P[sbc::OFF_MU + k] = (float)mu;
+        P[sbc::OFF_ISD + k] = var > 1e-12 ? (float)(1.0 / std::sqrt(var)) : 1.f;
+    }
+    CK(cudaMemcpyAsync(M->d_params, P.data(), sizeof(float) * P.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(M->d_m, 0, sizeof(float) * sbc::kTrainParams, s));
+    CK(cudaMemsetAsync(M->d_v, 0, sizeof(float) * sbc::kTrainParams, s));
+    CK(cudaMemsetAsync(M->d_grad, 0, sizeof(float) * sbc::kTrainParams, s));
+    M->adam_t = 0;
+    static const int64_t primes[] = {1000003, 2000003, 4000037, 16777259, 104729, 1299709, 15485863, 179424673};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, s));
+    const int64_t steps = ntr / batch;
+    for (int ep = 0; ep < epochs; ++ep) {
+        int64_t mul = 1;
+        for (int tries = 0; tries < 64; ++tries) {
+            const int64_t p = primes[(rng() >> 7) % (sizeof primes / sizeof primes[0])];
+            if (ntr % p) {
+                mul = p % ntr ? p : 1;
+                break;
+            }
+        }
+        const int64_t add = (int64_t)(rng() % (uint64_t)ntr);
+        for (int64_t k = 0; k < steps; ++k) CK(sbc::launch_train_step(f, k * batch, batch, ntr, mul, add, (float)lr));
+    }
+    CK(cudaEventRecord(e1, s));
+    CK(cudaMemsetAsync(M->d_sums, 0, sizeof(double) * 32, s));
+    CK(sbc::launch_eval(f, ntr, n, ymean));
+    CK(cudaMemcpyAsync(sums, M->d_sums, sizeof sums, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    M->trained = true;
+    drop_captured(f);
+    if (st) {
+        memset(st, 0, sizeof *st);
+        st->samples = n;
+        st->train_samples = ntr;
+        st->val_samples = nval;
+        st->epochs = epochs;
+        st->steps = steps * epochs;
+        st->train_ms = ms;
+        if (nval > 0) {
+            st->val_mae = sums[24] / (double)nval;
+            st->val_rmse = std::sqrt(sums[25] / (double)nval);
+            st->val_mae_mean = sums[26] / (double)nval;
+        }
+    }
+    return SBC_OK;
+}
+
+int sbc_forest_compare_schedules(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, int reps,
+                                 double* ms_static, double* ms_model)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_forest_compare_schedules: the forest's graph was destroyed");
+    if (!f || n <= 0 || !u || !v || reps < 0) return fail(SBC_ERR_ARG, "sbc_forest_compare_schedules: bad arguments");
+    if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_forest_compare_schedules before sbc_static_init");
+    if (!f->model || !f->model->trained)
+        return fail(SBC_ERR_STATE, "sbc_forest_compare_schedules: the cost model is not trained");
+    if (n >= INT32_MAX) return fail(SBC_ERR_ARG, "batch too large");
+    sbc_graph* g = f->g;
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    if (reps == 0) reps = 1;
+    int rc = plan_capacity(g, n, u, v, false);
+    if (rc) return rc;
+    if ((rc = stage_host(g, n, u, v, false))) return rc;
+    if ((rc = ensure_model_batch(f, g->ins_capacity))) return rc;
+    CK(sbc::launch_append(g, (int)n, false));
+    TrialState T;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    unsigned long long saved[SBC_NCOUNTERS];
+    const bool logging = f->model->logging;
+    const int schedule = f->schedule;
+    cudaError_t e;
+    auto cleanup = [&]() {
+        T.release();
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        f->model->logging = logging;
+        f->schedule = schedule;
+    };
+    if ((e = T.alloc(f, f->nk)) || (e = cudaEventCreate(&e0)) || (e = cudaEventCreate(&e1)) ||
+        (e = cudaMemcpyAsync(saved, f->d_counters, sizeof saved, cudaMemcpyDeviceToHost, g->stream)) ||
+        (e = cudaStreamSynchronize(g->stream))) {
+        cleanup();
+        return cuda_fail(e, "sbc_forest_compare_schedules setup");
+    }
+    f->model->logging = false;
+    double best[2] = {-1.0, -1.0};
+    for (int rep = 0; rep < reps; ++rep) {
+        for (int sch = 0; sch < 2; ++sch) {
+            f->schedule = sch;
+            e = T.copy_from(f, g->stream);
+            T.swap(f);
+            if (!e) e = cudaEventRecord(e0, g->stream);
+            if (!e) e = sbc::launch_update(f, (int)n, false);
+            if (!e) e = cudaEventRecord(e1, g->stream);
+            T.swap(f);
+            if (!e) e = cudaEventSynchronize(e1);
+            float t = 0.f;
+            if (!e) e = cudaEventElapsedTime(&t, e0, e1);
+            if (e) {
+                cleanup();
+                return cuda_fail(e, "sbc_forest_compare_schedules trial");
+            }
+            if (best[sch] < 0.0 || t < best[sch]) best[sch] = t;
+        }
+    }
+    cleanup();
+    CK(cudaMemcpyAsync(f->d_counters, saved, sizeof saved, cudaMemcpyHostToDevice, g->stream));
+    CK(sbc::launch_update(f, (int)n, false));
+    CK(sbc::launch_seal(g, (int)n));
+    if (ms_static) *ms_static = best[0];
+    if (ms_model) *ms_model = best[1];
+    return check_graph_err(g);
+}
+
+int sbc_set_schedule(sbc_forest* f, int schedule)
+{
+    if (!f || (schedule != SBC_SCHED_STATIC && schedule != SBC_SCHED_MODEL))
+        return fail(SBC_ERR_ARG, "sbc_set_schedule: bad arguments");
+    if (schedule == SBC_SCHED_MODEL && (!f->model || !f->model->trained))
+        return fail(SBC_ERR_STATE, "sbc_set_schedule: the cost model is not trained");
+    if (f->g && use_device(f->g->device)) return SBC_ERR_CUDA;
+    if (f->g) CK(cudaStreamSynchronize(f->g->stream));
+    f->schedule = schedule;
+    drop_captured(f);
+    return SBC_OK;
+}
+
+int sbc_cost_model_params(sbc_forest* f, float* get, const float* set)
+{
+    if (!f || !f->g) return fail(SBC_ERR_ARG, "sbc_cost_model_params: null forest or graph");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    int rc = ensure_model(f);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(f->g->stream));
+    if (set) {
+        CK(cudaMemcpy(f->model->d_params, set, sizeof(float) * sbc::kModelParams, cudaMemcpyHostToDevice));
+        f->model->trained = true;
+        drop_captured(f);
+    }
+    if (get) CK(cudaMemcpy(get, f->model->d_params, sizeof(float) * sbc::kModelParams, cudaMemcpyDeviceToHost));
+    return SBC_OK;
+}
+
+int sbc_cost_model_predict(sbc_forest* f, int64_t n, const float* x, float* out)
+{
+    if (!f || !f->g || !f->model || n < 0 || (n > 0 && (!x || !out)))
+        return fail(SBC_ERR_ARG, "sbc_cost_model_predict: bad arguments");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    if (n == 0) return SBC_OK;
+    float *dx = nullptr, *dout = nullptr;
+    cudaError_t e;
+    if ((e = dev_alloc(&dx, (size_t)n * sbc::kIn)) || (e = dev_alloc(&dout, (size_t)n)) ||
+        (e = cudaMemcpy(dx, x, sizeof(float) * n * sbc::kIn, cudaMemcpyHostToDevice)) ||
+        (e = sbc::launch_predict(f->model->d_params, dx, n, dout, f->g->stream)) ||
+        (e = cudaStreamSynchronize(f->g->stream)) ||
+        (e = cudaMemcpy(out, dout, sizeof(float) * n, cudaMemcpyDeviceToHost))) {
+        dev_free(dx);
+        dev_free(dout);
+        return cuda_fail(e, "sbc_cost_model_predict");
+    }
+    dev_free(dx);
+    dev_free(dout);
+    return SBC_OK;
+}
+
+int sbc_cost_model_grad(sbc_forest* f, int64_t n, const float* x, const float* y, float* grad, float* pred)
+{
+    if (!f || !f->g || !f->model || n <= 0 || n > 65536 || !x || !y || !grad)
+        return fail(SBC_ERR_ARG, "sbc_cost_model_grad: bad arguments");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    float *dx = nullptr, *dy = nullptr, *dg = nullptr, *dp = nullptr;
+    cudaError_t e;
+    cudaStream_t s = f->g->stream;
+    if ((e = dev_alloc(&dx, (size_t)n * sbc::kIn)) || (e = dev_alloc(&dy, (size_t)n)) ||
+        (e = dev_alloc(&dg, (size_t)sbc::kTrainParams)) || (e = dev_alloc(&dp, (size_t)n)) ||
+        (e = cudaMemcpy(dx, x, sizeof(float) * n * sbc::kIn, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(dy, y, sizeof(float) * n, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemsetAsync(dg, 0, sizeof(float) * sbc::kTrainParams, s)) ||
+        (e = sbc::launch_grad(f->model->d_params, dg, dx, dy, 0, n, n, 1, 0, dp, s)) ||
+        (e = cudaStreamSynchronize(s)) ||
+        (e = cudaMemcpy(grad, dg, sizeof(float) * sbc::kTrainParams, cudaMemcpyDeviceToHost)) ||
+        (pred && (e = cudaMemcpy(pred, dp, sizeof(float) * n, cudaMemcpyDeviceToHost)))) {
+        dev_free(dx), dev_free(dy), dev_free(dg), dev_free(dp);
+        return cuda_fail(e, "sbc_cost_model_grad");
+    }
+    dev_free(dx), dev_free(dy), dev_free(dg), dev_free(dp);
+    return SBC_OK;
+}
+
+int sbc_get_level_hist(sbc_forest* f, int64_t r0, int64_t nr, int32_t* out)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "state read: the forest's graph was destroyed");
+    if (!f || !out || r0 < 0 || nr < 0 || r0 + nr > f->nk) return fail(SBC_ERR_ARG, "level hist: bad row range");
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaMemcpyAsync(out, f->d_lvlhist + r0 * sbc::kHistLevels, sizeof(int32_t) * nr * sbc::kHistLevels,
+                       cudaMemcpyDeviceToHost, f->g->stream));
+    CK(cudaStreamSynchronize(f->g->stream));
+    return SBC_OK;
 }
 
 // ------------------------------------------------------------------ groups
@@ -1181,6 +1557,7 @@ int sbc_update_inserted(sbc_forest* f, int64_t n, const int64_t* u, const int64_
     }
     int rc = stage_host(g, n, u, v, true);
     if (rc) return rc;
+    if ((rc = ensure_model_batch(f, g->ins_capacity))) return rc;
     if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
     f->prof_begin(sbc::PROF_BATCH);
     CK(sbc::launch_update(f, (int)n, true));

@@ -16,6 +16,44 @@ enum ProfKernel { PROF_STATIC = 0, PROF_APPEND, PROF_CLASSIFY, PROF_UPDATE, PROF
 
 struct sbc_forest;
 
+namespace sbc {
+// Cost model: an FP32 MLP 8 -> 64 -> 64 -> 1 (ReLU) predicting log(1 + touched
+// vertices) of one (insertion, root) job.  Parameter layout in floats:
+constexpr int kIn = 8, kH = 64;
+constexpr int OFF_W1 = 0;                  // [kIn][kH]
+constexpr int OFF_B1 = OFF_W1 + kIn * kH;  // [kH]
+constexpr int OFF_W2 = OFF_B1 + kH;        // [kH][kH]
+constexpr int OFF_B2 = OFF_W2 + kH * kH;   // [kH]
+constexpr int OFF_W3 = OFF_B2 + kH;        // [kH]
+constexpr int OFF_B3 = OFF_W3 + kH;        // [1]
+constexpr int kTrainParams = OFF_B3 + 1;   // trained parameters
+constexpr int OFF_MU = kTrainParams;       // [kIn] feature means
+constexpr int OFF_ISD = OFF_MU + kIn;      // [kIn] inverse feature standard deviations
+constexpr int kModelParams = OFF_ISD + kIn;
+constexpr int kCostBuckets = 256;          // ordering buckets: 8 per doubling of predicted cost
+}  // namespace sbc
+
+// Training data, parameters and per-batch buffers of a forest's cost model.
+struct CostModel {
+    bool logging = false;   // log (features, touched vertices) of every job of later batches
+    bool trained = false;
+    int64_t capacity = 0;   // training samples the log holds
+    int adam_t = 0;
+    float* d_params = nullptr;  // [kModelParams]
+    float* d_m = nullptr;       // Adam moments [kTrainParams]
+    float* d_v = nullptr;
+    float* d_grad = nullptr;    // [kTrainParams]
+    float* d_x = nullptr;       // [capacity][kIn] features
+    float* d_y = nullptr;       // [capacity] log(1 + touched vertices)
+    unsigned long long* d_n = nullptr;  // samples appended (may exceed capacity; the excess is dropped)
+    double* d_sums = nullptr;   // [32] reduction accumulators
+    int64_t log_ins = 0;        // batch size the two per-batch buffers hold
+    float* d_feat = nullptr;    // [nk][log_ins][kIn] features of the batch's (root, insertion) pairs
+    int32_t* d_cost_log = nullptr;  // [nk][log_ins] touched vertices, -1 where no job ran
+    float* d_root_cost = nullptr;   // [nk] predicted touched vertices of the batch, -1 if culled
+    int* d_buckets = nullptr;       // [kCostBuckets]
+};
+
 // Scratch of a set of persistent update/static workers, each sized for nv
 // vertices: step/state word, queues and level offsets (int32), diffPath
 // (int64), delta accumulator (fp64) and one bitmap bit per vertex.  Zeroed on
@@ -140,6 +178,9 @@ struct sbc_forest {
     int64_t workers = 0;      // == ws.workers
     int64_t workers_req = 0;  // worker count the caller asked for (0 = one per resident CTA)
     int groups = 0;           // groups this forest is a member of
+    int32_t* d_lvlhist = nullptr;  // [nk][kHistLevels] vertices per level of each root's tree
+    CostModel* model = nullptr;    // allocated by the first cost-model call
+    int schedule = 0;              // root order of a batch: 0 static (classify order), 1 cost model
     int64_t state_bytes = 0;
     WorkerScratch ws;
     int* d_worklist = nullptr;
@@ -293,6 +334,8 @@ inline ForestSlot forest_slot(const sbc_forest* f, int n)
     s.ins_ok = g->d_ins + 2 * g->ins_capacity;
     s.nins = n;
     s.nk = (int)f->nk;
+    s.lvlhist = f->d_lvlhist;
+    s.cost_log = nullptr;
     return s;
 }
 
@@ -312,6 +355,25 @@ cudaError_t launch_set_src(sbc_graph* g, const int32_t* d_u, const int32_t* d_v)
 cudaError_t launch_stage(sbc_graph* g, int n);
 cudaError_t launch_seal(sbc_graph* g, int n);
 cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq);
+// Cost model and schedule (sbc_model.cu).
+cudaError_t launch_level_hist(sbc_forest* f);
+// Before the update of a batch of n: features of every active (root,
+// insertion) pair into the log buffers (when logging) and, under the model
+// schedule, the worklist ordered by predicted cost (longest first);
+// returns whether it built the worklist.
+cudaError_t launch_schedule(sbc_forest* f, int n, bool* built_worklist);
+// After the update: the batch's logged (features, cost) pairs into the training set.
+cudaError_t launch_log_append(sbc_forest* f, int n);
+cudaError_t launch_moments(sbc_forest* f, int64_t n);
+// Mean-squared-error gradient of samples at positions [base, base+count) of
+// the permutation j -> (j * mul + add) % n of (d_x, d_y), added into d_grad;
+// predictions into d_pred (may be null).
+cudaError_t launch_grad(const float* d_params, float* d_grad, const float* d_x, const float* d_y, int64_t base,
+                        int64_t count, int64_t n, int64_t mul, int64_t add, float* d_pred, cudaStream_t s);
+// launch_grad over the forest's training set, then one Adam step.
+cudaError_t launch_train_step(sbc_forest* f, int64_t base, int64_t count, int64_t n, int64_t mul, int64_t add, float lr);
+cudaError_t launch_eval(sbc_forest* f, int64_t lo, int64_t hi, float ymean);
+cudaError_t launch_predict(const float* d_params, const float* d_x, int64_t n, float* d_out, cudaStream_t s);
 int group_variant_count();
 int group_workers_per_sm(int v);
 // Append, classify + update, and seal (the steps selected) for the counts[s]

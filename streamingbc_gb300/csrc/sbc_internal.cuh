@@ -58,7 +58,12 @@ struct ForestSlot {
     const int32_t* ins_ok;
     int nins;
     int nk;
+    int32_t* lvlhist;   // [nk][kHistLevels] vertices per level (last bucket: that level and deeper), or null
+    int32_t* cost_log;  // [nk][nins] touched vertices of each job (cost-model training data), or null
 };
+
+// Levels tracked by the per-root level histograms (deeper levels share the last bucket).
+constexpr int kHistLevels = 64;
 
 struct Scratch {
     int32_t* st;

@@ -142,17 +142,24 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     sbc_graph* g = f->g;
     cudaStream_t s = g->stream;
     cudaError_t e;
-    if ((e = cudaMemsetAsync(f->d_nwork, 0, 2 * sizeof(int), s))) return e;  // nwork, counter
     const int32_t* iu = g->d_ins;
     const int32_t* iv = g->d_ins + g->ins_capacity;
     const int32_t* ok = g->d_ins + 2 * g->ins_capacity;
     f->prof_begin(PROF_CLASSIFY);
-    k_classify<<<(int)((f->nk + 255) / 256), 256, 0, s>>>(f->d_dist, f->nv, (int)f->nk, n, iu, iv, ok,
-                                                          f->d_worklist, f->d_nwork);
+    // cost-model features / ordered worklist (when the forest logs or is
+    // scheduled by the model), else the static classify order
+    bool ordered = false;
+    if ((e = launch_schedule(f, n, &ordered))) return e;
+    if (!ordered) {
+        if ((e = cudaMemsetAsync(f->d_nwork, 0, 2 * sizeof(int), s))) return e;  // nwork, counter
+        k_classify<<<(int)((f->nk + 255) / 256), 256, 0, s>>>(f->d_dist, f->nv, (int)f->nk, n, iu, iv, ok,
+                                                              f->d_worklist, f->d_nwork);
+    }
     f->prof_end(PROF_CLASSIFY);
     if ((e = cudaGetLastError())) return e;
     UpdateArgs A;
     A.f = forest_slot(f, n);
+    if (f->model && f->model->logging) A.f.cost_log = f->model->d_cost_log;
     A.scr = f->scratch();
     A.all_visible = all_visible ? 1 : 0;
     A.worklist = f->d_worklist;
@@ -163,7 +170,8 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     f->prof_begin(PROF_UPDATE);
     kVariants[f->variant].launch(A, grid, s);
     f->prof_end(PROF_UPDATE);
-    return cudaGetLastError();
+    if ((e = cudaGetLastError())) return e;
+    return launch_log_append(f, n);
 }
 
 }  // namespace sbc

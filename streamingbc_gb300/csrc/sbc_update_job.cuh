@@ -91,6 +91,12 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
             const int s = W.st[k];
             const int nl = Lb + (s & SBC_STEP_MASK) - 1;
             if (D[k] != nl) {
+                if (A.lvlhist) {
+                    int32_t* H = A.lvlhist + (size_t)r * kHistLevels;
+                    const int old = D[k];
+                    if (old != SBC_INF) atomicSub(&H[min(old, kHistLevels - 1)], 1);
+                    atomicAdd(&H[min(nl, kHistLevels - 1)], 1);
+                }
                 D[k] = nl;
                 D8[k] = enc_d8(nl);
                 W.st[k] = s | SBC_MOVED;
@@ -399,7 +405,10 @@ __device__ __forceinline__ void process_root(const ForestSlot& A, UpdSmem<NT>& s
             if (moving) c2++;
             else c1++;
         }
+        const unsigned long long walked0 = sm.lb.walked_v;  // read before run_job's first barrier
         run_job<NT>(A, sm, W, r, a, b, moving, all_visible ? INT_MAX : i);
+        if (A.cost_log && threadIdx.x == 0)
+            A.cost_log[(size_t)r * A.nins + i] = (int32_t)min(sm.lb.walked_v - walked0, (unsigned long long)INT_MAX);
     }
 }
 

@@ -22,11 +22,18 @@ INCLUDE = os.path.join(ROOT, "include")
 _i64p = C.POINTER(C.c_int64)
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
+_f32p = C.POINTER(C.c_float)
 _vp = C.c_void_p
 
 
 class SbcError(RuntimeError):
     pass
+
+
+class ModelStats(C.Structure):
+    _fields_ = [("samples", C.c_int64), ("train_samples", C.c_int64), ("val_samples", C.c_int64),
+                ("steps", C.c_int64), ("epochs", C.c_int), ("train_ms", C.c_double), ("val_mae", C.c_double),
+                ("val_rmse", C.c_double), ("val_mae_mean", C.c_double)]
 
 
 class BatchStats(C.Structure):
@@ -102,6 +109,18 @@ def load(path: str = LIB_PATH):
         "sbc_forest_variant": (C.c_int, [_vp, C.POINTER(C.c_int)]),
         "sbc_forest_autotune": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.c_int, C.POINTER(C.c_int), _f64p,
                                           C.c_int]),
+        "sbc_cost_model_size": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "sbc_cost_log_start": (C.c_int, [_vp, C.c_int64]),
+        "sbc_cost_log_stop": (C.c_int, [_vp, _i64p]),
+        "sbc_cost_log_read": (C.c_int, [_vp, C.c_int64, C.c_int64, _f32p, _f32p]),
+        "sbc_cost_model_train": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint64,
+                                           C.POINTER(ModelStats)]),
+        "sbc_set_schedule": (C.c_int, [_vp, C.c_int]),
+        "sbc_forest_compare_schedules": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.c_int, _f64p, _f64p]),
+        "sbc_cost_model_params": (C.c_int, [_vp, _f32p, _f32p]),
+        "sbc_cost_model_predict": (C.c_int, [_vp, C.c_int64, _f32p, _f32p]),
+        "sbc_cost_model_grad": (C.c_int, [_vp, C.c_int64, _f32p, _f32p, _f32p, _f32p]),
+        "sbc_get_level_hist": (C.c_int, [_vp, C.c_int64, C.c_int64, _i32p]),
         "sbc_group_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp), C.c_int]),
         "sbc_group_destroy": (C.c_int, [_vp]),
         "sbc_group_info": (C.c_int, [_vp, C.POINTER(C.c_int), _i64p, _i64p, C.POINTER(C.c_int)]),
@@ -239,6 +258,78 @@ class DeviceForest:
 
     def set_graph_capture(self, on: bool):
         _check(self.lib.sbc_set_graph_capture(self.h, 1 if on else 0))
+
+    # ---- cost model ----
+    SCHED_STATIC, SCHED_MODEL = 0, 1
+
+    def cost_log_start(self, capacity: int):
+        _check(self.lib.sbc_cost_log_start(self.h, int(capacity)))
+
+    def cost_log_stop(self) -> int:
+        n = C.c_int64(0)
+        _check(self.lib.sbc_cost_log_stop(self.h, C.byref(n)))
+        return n.value
+
+    def cost_log_read(self, first: int, count: int):
+        x = np.zeros((count, 8), dtype=np.float32)
+        y = np.zeros(count, dtype=np.float32)
+        _check(self.lib.sbc_cost_log_read(self.h, int(first), int(count), x.ctypes.data_as(_f32p),
+                                          y.ctypes.data_as(_f32p)))
+        return x, y
+
+    def train_cost_model(self, epochs=8, batch=4096, lr=2e-3, val_frac=0.1, seed=1) -> dict:
+        st = ModelStats()
+        _check(self.lib.sbc_cost_model_train(self.h, int(epochs), int(batch), float(lr), float(val_frac), int(seed),
+                                             C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ModelStats._fields_}
+
+    def set_schedule(self, schedule: int):
+        _check(self.lib.sbc_set_schedule(self.h, int(schedule)))
+
+    def compare_schedules(self, pairs, reps: int = 1):
+        """Insert `pairs` after timing its update under the static and the
+        model schedule on copies of the state; returns (ms_static, ms_model)."""
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        u = np.ascontiguousarray(pairs[:, 0])
+        v = np.ascontiguousarray(pairs[:, 1])
+        a, b = C.c_double(0), C.c_double(0)
+        _check(self.lib.sbc_forest_compare_schedules(self.h, len(u), p64(u), p64(v), int(reps), C.byref(a),
+                                                     C.byref(b)))
+        return a.value, b.value
+
+    def model_params(self, new=None) -> np.ndarray:
+        n = C.c_int(0)
+        _check(self.lib.sbc_cost_model_size(C.byref(n), None))
+        out = np.zeros(n.value, dtype=np.float32)
+        src = None
+        if new is not None:
+            src = np.ascontiguousarray(new, dtype=np.float32)
+            assert src.size == n.value
+        _check(self.lib.sbc_cost_model_params(self.h, out.ctypes.data_as(_f32p),
+                                              src.ctypes.data_as(_f32p) if src is not None else None))
+        return out
+
+    def model_predict(self, x) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 8)
+        out = np.zeros(len(x), dtype=np.float32)
+        _check(self.lib.sbc_cost_model_predict(self.h, len(x), x.ctypes.data_as(_f32p), out.ctypes.data_as(_f32p)))
+        return out
+
+    def model_grad(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, 8)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        n = C.c_int(0)
+        _check(self.lib.sbc_cost_model_size(C.byref(n), None))
+        g = np.zeros(n.value - 16, dtype=np.float32)
+        pred = np.zeros(len(x), dtype=np.float32)
+        _check(self.lib.sbc_cost_model_grad(self.h, len(x), x.ctypes.data_as(_f32p), y.ctypes.data_as(_f32p),
+                                            g.ctypes.data_as(_f32p), pred.ctypes.data_as(_f32p)))
+        return g, pred
+
+    def level_hist(self) -> np.ndarray:
+        out = np.zeros((self.nk, 64), dtype=np.int32)
+        _check(self.lib.sbc_get_level_hist(self.h, 0, self.nk, out.ctypes.data_as(_i32p)))
+        return out
 
     @property
     def variant(self) -> int:
