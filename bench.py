@@ -44,8 +44,13 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["rmat20", "rmat18", "rmat16", "chunglu40k", "er1024", "rmat_group64"],
-                   default="rmat20")
+    p.add_argument("--workload", choices=["rmat20", "rmat18", "rmat16", "chunglu40k", "er1024", "rmat_group64",
+                                          "serve16"], default="rmat20")
+    p.add_argument("--serve-rate", type=float, default=50000.0, help="serve16: offered insertions/s")
+    p.add_argument("--serve-requests", type=int, default=10000, help="serve16: timed requests")
+    p.add_argument("--serve-max-batch", type=int, default=1024)
+    p.add_argument("--serve-budget-gb", type=float, default=150.0)
+    p.add_argument("--plain-requests", type=int, default=10000, help="serve16: requests on the plain path")
     p.add_argument("--batch", type=int, default=64)
     p.add_argument("--group-batch", type=int, default=16,
                    help="rmat_group64: insertions per graph per step (64 graphs per step)")
@@ -247,6 +252,22 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
+    if args.workload == SERVE_WORKLOAD:
+        from streamingbc_gb300 import graphs as G
+        graphs = serving_set()
+        gid, pairs, _ = G.poisson_trace(graphs, args.serve_requests, args.serve_rate, seed=11)
+        cpu = cpu_sample_serve(graphs, gid, pairs, max(4, args.warmup + args.steps), threads)
+        value = cpu["value"]
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic", "impl": "reference",
+                "config": {"workload": SERVE_DESC.format(rate=args.serve_rate, budget=args.serve_budget_gb,
+                                                         mb=args.serve_max_batch),
+                           "step": "one insertion applied to all K roots of its graph"},
+                "cpu_baseline": cpu,
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload == GROUP_WORKLOAD:
         from streamingbc_gb300 import graphs as G
         specs = G.rmat_group(insertions=max(512, args.warmup + args.steps))
@@ -287,6 +308,151 @@ def run_reference(args):
                                        f"x{len(roots) / n_roots:g}, BC reduce added once"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+SERVE_WORKLOAD = "serve16"
+SERVE_DESC = ("serve16: 16 Chung-Lu graphs, n log-spaced 1e4..1e6, exponent 2.3, average degree 12, expected "
+              "degrees in [1, sqrt(2m)], seeds 200..215, LCC kept; K=512 uniform roots each; requests arrive as a "
+              "Poisson process of {rate:g}/s, graph chosen proportional to its edges, uniform non-edge insertions; "
+              "HBM admission budget {budget} GB; per-graph continuous batching up to {mb} requests")
+
+
+def _serve_graph_one(i):
+    """Graph i of the serving set (same construction as graphs.serving_graphs)."""
+    from streamingbc_gb300 import graphs as G
+    n = int(round(1e4 * 100.0 ** (i / 15)))
+    m = int(round(12 * n / 2))
+    g = G.chung_lu(n, m, 2.3, 1.0, float(np.sqrt(2.0 * m)), seed=200 + i)
+    return g, G.pick_roots(g.nv, min(g.nv, 512), seed=200 + i)
+
+
+def serving_set():
+    """The 16 serving graphs, generated in parallel (spawned workers, before
+    any CUDA call of this process)."""
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        return pool.map(_serve_graph_one, range(16))
+
+
+def cpu_sample_serve(graphs, gid, pairs, n_ins, threads):
+    """Oracle port per graph on min(K, 2*threads) roots and its first n_ins
+    requests; the mix's CPU rate weights each graph's per-insertion time by
+    its share of the requests."""
+    from oracle import oracle as orc
+    orc.build()
+    share = np.bincount(gid, minlength=len(graphs)) / len(gid)
+    per = []
+    for i, (g, roots) in enumerate(graphs):
+        mine = pairs[gid == i][:n_ins]
+        if not len(mine):
+            per.append(0.0)
+            continue
+        nr = min(len(roots), 2 * threads)
+        o = orc.PortOracle(g.nv, g.off, g.adj, roots[:nr], nthreads=threads)
+        o.static_timed()
+        ts = []
+        for u, v in mine:
+            tr, tb = o.insert_timed(int(u), int(v))
+            ts.append(tr * (len(roots) / nr) + tb)
+        o.close()
+        per.append(float(np.mean(ts)))
+    t_mix = float(np.dot(share, per))
+    return {"value": 1.0 / t_mix, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"every graph: min(K, {2 * threads}) roots, first {n_ins} of its requests; per-root time "
+                      f"scaled to K, BC reduce added; mix weighted by request share"}
+
+
+def run_serve(args):
+    """Serving loop over 16 resident graphs: a Poisson trace played in real
+    time into the batched server, then a prefix of it into the plain server
+    (one request per batch)."""
+    rank, world, local = dist_env()
+    t0 = time.time()
+    graphs = serving_set()
+    gen_s = time.time() - t0
+    import torch
+    from streamingbc_gb300 import build as b
+    from streamingbc_gb300 import graphs as G
+    from streamingbc_gb300 import native
+    if not os.path.exists(native.LIB_PATH):
+        b.build()
+    lib = native.load()
+    lib.sbc_set_device(local if world > 1 else 0)
+    torch.cuda.set_device(local if world > 1 else 0)
+    rate = args.serve_rate
+    n_warm = 200 * max(args.warmup, 1)
+    n_req = args.serve_requests
+    gid, pairs, t = G.poisson_trace(graphs, n_warm + n_req + args.plain_requests, rate, seed=11)
+    budget = int(args.serve_budget_gb * (1 << 30))
+
+    def serve(max_batch, lo, hi, warm_hi, max_inflight=0):
+        srv = native.DeviceServer(budget_bytes=budget, max_batch=max_batch, max_inflight=max_inflight)
+        ids = [srv.add_graph(g, roots) for g, roots in graphs]
+        t1 = time.time()
+        srv.drain()  # admission + static init of every graph that fits
+        admit_s = time.time() - t1
+        if warm_hi > lo:
+            srv.play(gid[lo:warm_hi], pairs[lo:warm_hi], t[lo:warm_hi] - t[lo])
+            srv.drain()
+            srv.stats(reset=True)
+        clk = ClockSampler(local)
+        clk.start()
+        t1 = time.perf_counter()
+        srv.play(gid[warm_hi:hi], pairs[warm_hi:hi], t[warm_hi:hi] - t[warm_hi])
+        srv.drain()
+        wall = time.perf_counter() - t1
+        clocks = clk.stop()
+        st = srv.stats()
+        info = [srv.graph_info(i) for i in ids]
+        srv.close()
+        return st, wall, admit_s, clocks, info
+
+    st, wall, admit_s, clocks, info = serve(args.serve_max_batch, 0, n_warm + n_req, n_warm)
+    plain = None
+    if args.plain_requests:
+        lo = n_warm + n_req
+        pst, pwall, _, _, _ = serve(1, lo, lo + args.plain_requests, lo, max_inflight=1)
+        plain = {"value": pst["throughput"], "unit": UNIT, "requests": args.plain_requests,
+                 "p50_ms": pst["p50_us"] / 1e3, "p99_ms": pst["p99_us"] / 1e3, "wall_s": pwall,
+                 "note": "same graphs, arrival process and rate; one insertion at a time over all graphs "
+                         "(max_batch 1, one batch in flight): the unbatched plain GPU path"}
+        cst, cwall, _, _, _ = serve(1, lo, lo + args.plain_requests, lo)
+        plain["concurrent_graphs"] = {"value": cst["throughput"], "p50_ms": cst["p50_us"] / 1e3,
+                                      "p99_ms": cst["p99_us"] / 1e3,
+                                      "note": "one insertion per batch, but graphs overlap on the device"}
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        cpu = cpu_sample_serve(graphs, gid[n_warm:n_warm + n_req], pairs[n_warm:n_warm + n_req], 4,
+                               os.cpu_count() or 1)
+    if rank == 0:
+        value = st["throughput"]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": int(st["batches"]),
+            "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(st["batches"], 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64+f64", "data": "synthetic",
+            "config": {"workload": SERVE_DESC.format(rate=rate, budget=args.serve_budget_gb, mb=args.serve_max_batch),
+                       "graphs": len(graphs), "vertices": sum(g.nv for g, _ in graphs),
+                       "requests": n_req, "warmup_requests": n_warm, "offered_rate": rate,
+                       "admitted": sum(1 for x in info if x["state"] == "admitted"),
+                       "bytes_admitted": st["bytes_admitted"], "admission_s": admit_s, "generate_s": gen_s,
+                       "step": "one launched per-graph batch",
+                       "timing": "arrival (scheduled trace time) to batch completion (stream callback); value = "
+                                 "completed / (last completion - first arrival)"},
+            "latency_ms": {"p50": st["p50_us"] / 1e3, "p99": st["p99_us"] / 1e3, "mean": st["mean_us"] / 1e3,
+                           "max": st["max_us"] / 1e3},
+            "mean_batch": st["mean_batch"],
+            "per_graph_batches": [x["batches"] for x in info],
+            "roofline": None,
+            "cpu_baseline": cpu,
+            "e2e": {"value": st["completed"] / wall, "unit": UNIT, "h2d_bytes_per_step": 24 * st["mean_batch"],
+                    "d2h_bytes_per_step": 0, "note": "host requests in, results resident on the device; wall time "
+                                                      "of play + drain"},
+            "clocks": clocks,
+            "gpu_launches": int(st["batches"]) * 4,  # append, classify, update, seal per batch
+            "plain_gpu": plain,
+            "batched_over_plain": value / plain["value"] if plain and plain["value"] else None,
+        }
+        print(json.dumps(line), flush=True)
 
 
 def run_group(args):
@@ -640,6 +806,8 @@ def main():
         run_reference(args)
     elif args.workload == GROUP_WORKLOAD:
         run_group(args)
+    elif args.workload == SERVE_WORKLOAD:
+        run_serve(args)
     else:
         run_ours(args)
 

@@ -128,6 +128,13 @@ int sbc_static_init(sbc_forest *f);
  * loops are rejected and counted, not applied.  Synchronous; stats may be NULL. */
 int sbc_insert_batch(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, sbc_batch_stats *stats);
 
+/* As sbc_insert_batch, but returns once the batch is queued on the graph's
+ * stream (no statistics): the endpoints are copied into the graph's pinned
+ * staging before return, so u and v may be reused at once; a later batch on
+ * the same graph waits only until this one's staging copies have run.
+ * sbc_sync waits for completion and reports slack errors. */
+int sbc_insert_batch_async(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v);
+
 /* As sbc_insert_batch, with int32 vertex ids already in DEVICE memory; returns
  * without synchronising (results are ordered on the graph's stream).  Slack for
  * these insertions must have been reserved with sbc_graph_reserve; an insertion
@@ -244,6 +251,59 @@ int sbc_group_autotune(sbc_group *G, const int64_t *counts, const int64_t *u, co
                        int *chosen, double *ms, int ms_len);
 int sbc_group_read_counters(sbc_group *G, int64_t *vertices, int64_t *edges, int64_t *case1, int64_t *case2,
                             int64_t *scanned);
+
+/* ---- serving loop ---------------------------------------------------------
+ * A server keeps many graphs (each with its forest of K roots) resident on
+ * one device and batches insertion requests per graph as they arrive; the
+ * reference's callers apply one insertion at a time (src/sbcMain_utils.c:
+ * 458-471, src/streamingbc.c:56-77).  Graphs are admitted in registration
+ * order while the sum of their estimated device footprints (adjacency,
+ * per-root state, worker scratch) fits hbm_budget_bytes; requests for a graph
+ * not yet admitted wait in its queue.  A scheduler thread launches, for every
+ * graph with queued requests and no batch on the device, all of them (up to
+ * max_batch) as its next batch on the graph's own stream, so graphs overlap on
+ * the device and requests arriving meanwhile join the next batch.  Latency is
+ * measured from each request's arrival to its batch's completion.  Per-graph
+ * order is kept, so every graph ends where applying its own stream alone ends. */
+typedef struct sbc_server sbc_server;
+typedef struct {
+    int64_t submitted, completed, batches, graphs_admitted, graphs_waiting;
+    double p50_us, p99_us, mean_us, max_us;  /* arrival -> batch completion */
+    double throughput;      /* completed / (last completion - first arrival), insertions/s */
+    double mean_batch;      /* requests per launched batch */
+    int64_t bytes_admitted, bytes_budget;
+} sbc_server_stats;
+int sbc_server_create(sbc_server **out, int device, int64_t hbm_budget_bytes, int max_batch);
+int sbc_server_destroy(sbc_server *s);
+/* At most max_inflight batches on the device at once over all graphs (0, the
+ * default, means no limit); graphs are served round-robin.  max_batch 1 with
+ * max_inflight 1 is the plain path: one insertion at a time. */
+int sbc_server_set_max_inflight(sbc_server *s, int max_inflight);
+/* Register a graph (symmetric CSR, copied) with nk roots; variant -1 picks the
+ * update launch shape by size.  *id is its index (0, 1, ...). */
+int sbc_server_add_graph(sbc_server *s, int64_t nv, const int64_t *off, const int64_t *adj, int64_t nk,
+                         const int64_t *roots, int variant, int *id);
+/* state: 0 waiting for admission, 1 admitted, 2 released. */
+int sbc_server_graph_info(sbc_server *s, int id, int *state, int64_t *footprint_bytes, int64_t *completed,
+                          int64_t *batches);
+/* One insertion request (arrival time = now).  Thread-safe. */
+int sbc_server_submit(sbc_server *s, int id, int64_t u, int64_t v);
+/* Trace player: request i (graph[i], u[i], v[i]) arrives t_offset_s[i]
+ * seconds after the call (non-decreasing); returns once all are submitted. */
+int sbc_server_play(sbc_server *s, int64_t n, const int32_t *graph, const int64_t *u, const int64_t *v,
+                    const double *t_offset_s);
+/* Wait until every admitted graph's static init and submitted requests have
+ * completed and no release or admission is left to carry out (requests of
+ * graphs that do not fit the budget yet stay queued). */
+int sbc_server_drain(sbc_server *s);
+const char *sbc_server_error(sbc_server *s);
+/* Free graph id's device memory once its queue is empty (waiting graphs may
+ * then be admitted); later requests for it are refused. */
+int sbc_server_release(sbc_server *s, int id);
+/* Results of an idle admitted graph (any pointer may be NULL):
+ * dist[nk][nv], sigma[nk][nv], bc[nv]. */
+int sbc_server_read(sbc_server *s, int id, int32_t *dist, int64_t *sigma, double *bc);
+int sbc_server_get_stats(sbc_server *s, sbc_server_stats *stats, int reset);
 
 /* Wait for all work queued on the forest's graph stream. */
 int sbc_sync(sbc_forest *f);

@@ -78,6 +78,7 @@ int ensure_staging(sbc_graph* g, int64_t n)
 {
     if (n <= g->ins_capacity) return SBC_OK;
     int cap = (int)std::max<int64_t>(n, 64);
+    CK(cudaStreamSynchronize(g->stream));  // queued batches may still read the old staging
     if (g->d_ins) cudaFree(g->d_ins);
     if (g->h_ins) cudaFreeHost(g->h_ins);
     g->d_ins = nullptr;
@@ -164,6 +165,7 @@ int stage_host(sbc_graph* g, int64_t n, const int64_t* u, const int64_t* v, bool
     int rc = ensure_staging(g, n);
     if (rc) return rc;
     const int cap = g->ins_capacity;
+    if (g->staged) CK(cudaEventSynchronize(g->staged));  // the previous batch's copies out of h_ins are done
     int32_t* hu = g->h_ins;
     int32_t* hv = g->h_ins + cap;
     int32_t* hok = g->h_ins + 2 * cap;
@@ -181,6 +183,7 @@ int stage_host(sbc_graph* g, int64_t n, const int64_t* u, const int64_t* v, bool
     CK(cudaMemcpyAsync(g->d_ins, hu, sizeof(int32_t) * n, cudaMemcpyHostToDevice, g->stream));
     CK(cudaMemcpyAsync(g->d_ins + cap, hv, sizeof(int32_t) * n, cudaMemcpyHostToDevice, g->stream));
     if (set_ok) CK(cudaMemcpyAsync(g->d_ins + 2 * cap, hok, sizeof(int32_t) * n, cudaMemcpyHostToDevice, g->stream));
+    CK(cudaEventRecord(g->staged, g->stream));
     return SBC_OK;
 }
 
@@ -595,7 +598,8 @@ int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int6
     }
 
     cudaError_t e;
-    if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) || (e = dev_alloc(&g->d_row, nv + 1)) ||
+    if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) ||
+        (e = cudaEventCreateWithFlags(&g->staged, cudaEventDisableTiming)) || (e = dev_alloc(&g->d_row, nv + 1)) ||
         (e = dev_alloc(&g->d_deg, nv)) || (e = dev_alloc(&g->d_deg0, nv)) || (e = dev_alloc(&g->d_cap, nv)) ||
         (e = dev_alloc(&g->d_nsort, nv)) ||
         (e = dev_alloc(&g->d_col, total)) || (e = dev_alloc(&g->d_seq, total)) || (e = dev_alloc(&g->d_err, 1)) ||
@@ -639,6 +643,7 @@ int sbc_graph_destroy(sbc_graph* g)
     dev_free(g->d_src);
     dev_free(g->d_ins);
     if (g->h_ins) cudaFreeHost(g->h_ins);
+    if (g->staged) cudaEventDestroy(g->staged);
     if (g->stream) cudaStreamDestroy(g->stream);
     delete g;
     return SBC_OK;
@@ -872,6 +877,25 @@ int sbc_insert_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* 
     f->prof_end(sbc::PROF_BATCH);
     if ((rc = collect_stats(f, n, stats))) return rc;
     return check_graph_err(g);
+}
+
+int sbc_insert_batch_async(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_insert_batch_async: the forest's graph was destroyed");
+    if (!f || n < 0 || (n > 0 && (!u || !v))) return fail(SBC_ERR_ARG, "sbc_insert_batch_async: bad arguments");
+    if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_insert_batch_async before sbc_static_init");
+    if (n >= INT32_MAX) return fail(SBC_ERR_ARG, "batch too large");
+    if (n == 0) return SBC_OK;
+    sbc_graph* g = f->g;
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    int rc = plan_capacity(g, n, u, v, false);
+    if (rc) return rc;
+    if ((rc = stage_host(g, n, u, v, false))) return rc;
+    if ((rc = ensure_model_batch(f, g->ins_capacity))) return rc;
+    CK(sbc::launch_append(g, (int)n, false));
+    CK(sbc::launch_update(f, (int)n, false));
+    CK(sbc::launch_seal(g, (int)n));
+    return SBC_OK;
 }
 
 int sbc_insert_batch_device(sbc_forest* f, int64_t n, const int32_t* d_u, const int32_t* d_v)

@@ -140,7 +140,8 @@ struct sbc_graph {
     // staging for insertion batches
     int ins_capacity = 0;
     int32_t* d_ins = nullptr;  // [3 * ins_capacity]: u, v, ok
-    int32_t* h_ins = nullptr;  // pinned [2 * ins_capacity]
+    int32_t* h_ins = nullptr;  // pinned [3 * ins_capacity]
+    cudaEvent_t staged = nullptr;  // recorded after the last copy out of h_ins
     const int32_t** d_src = nullptr;  // device slot: addresses of the caller's endpoint arrays
     int64_t repacks = 0;
     // forests bound to this graph; destroying the graph detaches them

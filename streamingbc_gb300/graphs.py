@@ -330,6 +330,41 @@ def rmat_group(count: int = 64, scale_lo: int = 10, scale_hi: int = 16, edge_fac
     return out
 
 
+def serving_graphs(count: int = 16, n_lo: float = 1e4, n_hi: float = 1e6, gamma: float = 2.3,
+                   avg_degree: float = 12.0, seed0: int = 200, k: int = 512):
+    """Graphs for the serving loop: Chung-Lu graph i has n_i = n_lo *
+    (n_hi/n_lo)^(i/(count-1)) vertices (log-spaced), m = avg_degree * n_i / 2
+    expected edges, power-law exponent gamma, expected degrees in
+    [1, sqrt(2m)] (the structural cutoff), seed seed0 + i; the largest
+    connected component is kept.  K = min(|V|, k) uniform roots each.
+    Returns a list of (graph, roots)."""
+    out = []
+    for i in range(count):
+        n = int(round(n_lo * (n_hi / n_lo) ** (i / max(count - 1, 1))))
+        m = int(round(avg_degree * n / 2))
+        g = chung_lu(n, m, gamma, 1.0, float(np.sqrt(2.0 * m)), seed=seed0 + i)
+        out.append((g, pick_roots(g.nv, min(g.nv, k), seed=seed0 + i)))
+    return out
+
+
+def poisson_trace(graphs, count: int, rate: float, seed: int):
+    """`count` insertion requests arriving as a Poisson process of `rate` per
+    second; each targets graph i with probability proportional to its edge
+    count and is a uniformly random non-edge of that graph (distinct within
+    the graph's stream).  Returns (graph ids int32, pairs [count][2] int64,
+    arrival offsets in seconds)."""
+    rng = np.random.default_rng(seed)
+    w = np.array([g.ne for g, _ in graphs], dtype=np.float64)
+    gid = rng.choice(len(graphs), size=count, p=w / w.sum()).astype(np.int32)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    pairs = np.zeros((count, 2), dtype=np.int64)
+    for i, (g, _) in enumerate(graphs):
+        sel = np.nonzero(gid == i)[0]
+        if sel.size:
+            pairs[sel] = uniform_insertions(g, sel.size, seed=seed * 1000 + i)
+    return gid, pairs, t
+
+
 def workload(name: str, small: bool = False):
     """(graph, roots, insertions) for a named workload.
 

@@ -30,6 +30,14 @@ class SbcError(RuntimeError):
     pass
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("batches", C.c_int64),
+                ("graphs_admitted", C.c_int64), ("graphs_waiting", C.c_int64), ("p50_us", C.c_double),
+                ("p99_us", C.c_double), ("mean_us", C.c_double), ("max_us", C.c_double),
+                ("throughput", C.c_double), ("mean_batch", C.c_double), ("bytes_admitted", C.c_int64),
+                ("bytes_budget", C.c_int64)]
+
+
 class ModelStats(C.Structure):
     _fields_ = [("samples", C.c_int64), ("train_samples", C.c_int64), ("val_samples", C.c_int64),
                 ("steps", C.c_int64), ("epochs", C.c_int), ("train_ms", C.c_double), ("val_mae", C.c_double),
@@ -121,6 +129,20 @@ def load(path: str = LIB_PATH):
         "sbc_cost_model_predict": (C.c_int, [_vp, C.c_int64, _f32p, _f32p]),
         "sbc_cost_model_grad": (C.c_int, [_vp, C.c_int64, _f32p, _f32p, _f32p, _f32p]),
         "sbc_get_level_hist": (C.c_int, [_vp, C.c_int64, C.c_int64, _i32p]),
+        "sbc_insert_batch_async": (C.c_int, [_vp, C.c_int64, _i64p, _i64p]),
+        "sbc_server_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.c_int64, C.c_int]),
+        "sbc_server_destroy": (C.c_int, [_vp]),
+        "sbc_server_set_max_inflight": (C.c_int, [_vp, C.c_int]),
+        "sbc_server_add_graph": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.c_int64, _i64p, C.c_int,
+                                           C.POINTER(C.c_int)]),
+        "sbc_server_graph_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), _i64p, _i64p, _i64p]),
+        "sbc_server_submit": (C.c_int, [_vp, C.c_int, C.c_int64, C.c_int64]),
+        "sbc_server_play": (C.c_int, [_vp, C.c_int64, _i32p, _i64p, _i64p, _f64p]),
+        "sbc_server_drain": (C.c_int, [_vp]),
+        "sbc_server_error": (C.c_char_p, [_vp]),
+        "sbc_server_release": (C.c_int, [_vp, C.c_int]),
+        "sbc_server_read": (C.c_int, [_vp, C.c_int, _i32p, _i64p, _f64p]),
+        "sbc_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats), C.c_int]),
         "sbc_group_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp), C.c_int]),
         "sbc_group_destroy": (C.c_int, [_vp]),
         "sbc_group_info": (C.c_int, [_vp, C.POINTER(C.c_int), _i64p, _i64p, C.POINTER(C.c_int)]),
@@ -251,6 +273,13 @@ class DeviceForest:
         st = BatchStats()
         _check(self.lib.sbc_insert_batch(self.h, u.size, p64(u), p64(v), C.byref(st)))
         return st.as_dict()
+
+    def insert_async(self, pairs):
+        """Queue a batch from host pairs without waiting (sync() waits)."""
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        u = np.ascontiguousarray(pairs[:, 0])
+        v = np.ascontiguousarray(pairs[:, 1])
+        _check(self.lib.sbc_insert_batch_async(self.h, u.size, p64(u), p64(v)))
 
     def insert_device(self, n: int, d_u: int, d_v: int):
         """Asynchronous batch from int32 device pointers (e.g. tensor.data_ptr())."""
@@ -496,6 +525,86 @@ class DeviceGroup:
     def close(self):
         if getattr(self, "h", None):
             self.lib.sbc_group_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceServer:
+    """sbc_server: graphs resident on one device, insertion requests batched
+    per graph as they arrive (admission by HBM footprint)."""
+
+    def __init__(self, budget_bytes: int, max_batch: int = 256, device: int = 0, max_inflight: int = 0):
+        self.lib = load()
+        h = _vp()
+        _check(self.lib.sbc_server_create(C.byref(h), int(device), int(budget_bytes), int(max_batch)))
+        self.h = h
+        self._shape = {}
+        if max_inflight:
+            self._rc(self.lib.sbc_server_set_max_inflight(self.h, int(max_inflight)))
+
+    def _rc(self, rc: int):
+        if rc != 0:
+            msg = self.lib.sbc_server_error(self.h).decode() or (_lib.sbc_last_error().decode() if _lib else "")
+            raise SbcError(f"sbc server error {rc}: {msg}")
+
+    def add_graph(self, g, roots, variant: int = -1) -> int:
+        off, adj, roots = _a64(g.off), _a64(g.adj), _a64(roots)
+        gid = C.c_int(-1)
+        self._rc(self.lib.sbc_server_add_graph(self.h, int(g.nv), p64(off), p64(adj), roots.size, p64(roots),
+                                               int(variant), C.byref(gid)))
+        self._shape[gid.value] = (int(g.nv), int(roots.size))
+        return gid.value
+
+    def graph_info(self, gid: int) -> dict:
+        st = C.c_int(0)
+        fp, done, nb = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        self._rc(self.lib.sbc_server_graph_info(self.h, int(gid), C.byref(st), C.byref(fp), C.byref(done),
+                                                C.byref(nb)))
+        return {"state": ("waiting", "admitted", "released")[st.value], "footprint": fp.value,
+                "completed": done.value, "batches": nb.value}
+
+    def submit(self, gid: int, u: int, v: int):
+        self._rc(self.lib.sbc_server_submit(self.h, int(gid), int(u), int(v)))
+
+    def play(self, gids, pairs, t_offsets):
+        """Submit request i at t_offsets[i] seconds after the call (native
+        timing loop); returns when all are submitted."""
+        gids = np.ascontiguousarray(gids, dtype=np.int32)
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        u = np.ascontiguousarray(pairs[:, 0])
+        v = np.ascontiguousarray(pairs[:, 1])
+        t = np.ascontiguousarray(t_offsets, dtype=np.float64)
+        self._rc(self.lib.sbc_server_play(self.h, len(gids), gids.ctypes.data_as(_i32p), p64(u), p64(v),
+                                          t.ctypes.data_as(_f64p)))
+
+    def drain(self):
+        self._rc(self.lib.sbc_server_drain(self.h))
+
+    def release(self, gid: int):
+        self._rc(self.lib.sbc_server_release(self.h, int(gid)))
+
+    def read(self, gid: int):
+        nv, nk = self._shape[gid]
+        dist = np.zeros((nk, nv), dtype=np.int32)
+        sigma = np.zeros((nk, nv), dtype=np.int64)
+        bc = np.zeros(nv, dtype=np.float64)
+        self._rc(self.lib.sbc_server_read(self.h, int(gid), dist.ctypes.data_as(_i32p), sigma.ctypes.data_as(_i64p),
+                                          bc.ctypes.data_as(_f64p)))
+        return dist, sigma, bc
+
+    def stats(self, reset: bool = False) -> dict:
+        st = ServerStats()
+        self._rc(self.lib.sbc_server_get_stats(self.h, C.byref(st), 1 if reset else 0))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sbc_server_destroy(self.h)
             self.h = None
 
     def __del__(self):
