@@ -179,7 +179,8 @@ int sbc_update_inserted(sbc_forest *f, int64_t n, const int64_t *u, const int64_
  * count) predicts log(1 + touched vertices) of each (insertion, root) job
  * from features taken at batch start: d(r,a), d(r,b) for the shallower and
  * deeper endpoint (64 = unreachable), their level difference, log1p of
- * deg(a), deg(b), sigma(r,a), sigma(r,b), and log1p of the number of vertices
+ * deg(a), deg(b), |sigma(r,a)|, |sigma(r,b)| (sigma wraps like the reference's
+ * int64), and log1p of the number of vertices
  * at level d(r,a)+1 of r's tree.  Under SBC_SCHED_MODEL each batch's active
  * roots are queued longest predicted batch cost first; SBC_SCHED_STATIC
  * (the default and the fallback) keeps the classify order.  Results never
@@ -225,6 +226,12 @@ int sbc_cost_model_grad(sbc_forest *f, int64_t n, const float *x, const float *y
 /* Per-root level histograms rows [r0, r0+nr): 64 counts each (the last
  * counts level 63 and deeper). */
 int sbc_get_level_hist(sbc_forest *f, int64_t r0, int64_t nr, int32_t *out);
+/* Roster of level `level` (2..15) of root row r: the members of a level with at
+ * most 256 vertices, kept for finding parents by lookup instead of adjacency
+ * scans (after each batch it holds exactly the level's members).  *n = -1 if
+ * the level is not tracked (too large, or rosters disabled); out holds up to
+ * 256 entries and may be NULL. */
+int sbc_get_roster(sbc_forest *f, int64_t r, int level, int32_t *out, int *n);
 
 /* ---- groups: many forests updated by one launch per batch --------------
  * The reference updates one forest per insertEdgeStreamingBC call

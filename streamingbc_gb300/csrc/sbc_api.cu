@@ -406,6 +406,7 @@ struct TrialState {
     double* delta = nullptr;
     double* bc = nullptr;
     int32_t* hist = nullptr;
+    int32_t *roster = nullptr, *roster_n = nullptr, *roster_dirty = nullptr;
     cudaError_t alloc(const sbc_forest* f, int64_t rows)
     {
         nk = rows;
@@ -413,7 +414,10 @@ struct TrialState {
         cudaError_t e;
         if ((e = dev_alloc(&dist, cells)) || (e = dev_alloc(&dist8, cells)) || (e = dev_alloc(&sigma, cells)) ||
             (e = dev_alloc(&delta, cells)) || (e = dev_alloc(&bc, f->nv)) ||
-            (f->d_lvlhist && (e = dev_alloc(&hist, (size_t)rows * sbc::kHistLevels))))
+            (f->d_lvlhist && (e = dev_alloc(&hist, (size_t)rows * sbc::kHistLevels))) ||
+            (f->d_roster && ((e = dev_alloc(&roster, (size_t)rows * sbc::kRosterLevels * sbc::kRosterCap)) ||
+                             (e = dev_alloc(&roster_n, (size_t)rows * sbc::kRosterLevels)) ||
+                             (e = dev_alloc(&roster_dirty, (size_t)rows * sbc::kRosterLevels)))))
             release();
         return e;
     }
@@ -425,6 +429,9 @@ struct TrialState {
         dev_free(delta);
         dev_free(bc);
         dev_free(hist);
+        dev_free(roster);
+        dev_free(roster_n);
+        dev_free(roster_dirty);
     }
     cudaError_t copy_from(const sbc_forest* f, cudaStream_t s) const
     {
@@ -436,7 +443,13 @@ struct TrialState {
             (e = cudaMemcpyAsync(sigma, f->d_sigma, sizeof(int64_t) * cells, d2d, s)) ||
             (e = cudaMemcpyAsync(delta, f->d_delta, sizeof(double) * cells, d2d, s)) ||
             (e = cudaMemcpyAsync(bc, f->d_bc, sizeof(double) * f->nv, d2d, s)) ||
-            (hist && (e = cudaMemcpyAsync(hist, f->d_lvlhist, sizeof(int32_t) * (size_t)nk * sbc::kHistLevels, d2d, s))))
+            (hist && (e = cudaMemcpyAsync(hist, f->d_lvlhist, sizeof(int32_t) * (size_t)nk * sbc::kHistLevels, d2d, s))) ||
+            (roster && ((e = cudaMemcpyAsync(roster, f->d_roster,
+                                             sizeof(int32_t) * (size_t)nk * sbc::kRosterLevels * sbc::kRosterCap, d2d, s)) ||
+                        (e = cudaMemcpyAsync(roster_n, f->d_roster_n, sizeof(int32_t) * (size_t)nk * sbc::kRosterLevels,
+                                             d2d, s)) ||
+                        (e = cudaMemcpyAsync(roster_dirty, f->d_roster_dirty,
+                                             sizeof(int32_t) * (size_t)nk * sbc::kRosterLevels, d2d, s)))))
             return e;
         return cudaSuccess;
     }
@@ -448,6 +461,11 @@ struct TrialState {
         std::swap(f->d_delta, delta);
         std::swap(f->d_bc, bc);
         if (hist) std::swap(f->d_lvlhist, hist);
+        if (roster) {
+            std::swap(f->d_roster, roster);
+            std::swap(f->d_roster_n, roster_n);
+            std::swap(f->d_roster_dirty, roster_dirty);
+        }
         std::swap(f->nk, nk);
     }
 };
@@ -781,7 +799,16 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
         return cuda_fail(e, "sbc_forest_create state allocation");
     }
     f->d_counter = f->d_nwork + 1;
-    f->state_bytes = (int64_t)(cells * 21 + f->nv * 8);
+    // rosters (16 KB per root) unless they would take more than 1 GB
+    const size_t roster_cells = (size_t)nk * sbc::kRosterLevels * sbc::kRosterCap;
+    if (roster_cells * 4 <= ((size_t)1 << 30) &&
+        ((e = dev_alloc(&f->d_roster, roster_cells)) ||
+         (e = dev_alloc(&f->d_roster_n, (size_t)nk * sbc::kRosterLevels)) ||
+         (e = dev_alloc(&f->d_roster_dirty, (size_t)nk * sbc::kRosterLevels)))) {
+        sbc_forest_destroy(f);
+        return cuda_fail(e, "sbc_forest_create roster allocation");
+    }
+    f->state_bytes = (int64_t)(cells * 21 + f->nv * 8 + (f->d_roster ? roster_cells * 4 : 0));
     f->workers_req = workers;
     int rc = alloc_scratch(f, variant);
     if (rc) {
@@ -819,6 +846,9 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_nwork);
     dev_free(f->d_counters);
     dev_free(f->d_lvlhist);
+    dev_free(f->d_roster);
+    dev_free(f->d_roster_n);
+    dev_free(f->d_roster_dirty);
     free_model(f);
     free_scratch(f);
     f->prof_release();
@@ -846,6 +876,7 @@ int sbc_static_init(sbc_forest* f)
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(sbc::launch_static(f));
     CK(sbc::launch_level_hist(f));
+    CK(sbc::launch_roster_build(f));
     f->initialized = true;
     return SBC_OK;
 }
@@ -1335,6 +1366,26 @@ int sbc_cost_model_grad(sbc_forest* f, int64_t n, const float* x, const float* y
         return cuda_fail(e, "sbc_cost_model_grad");
     }
     dev_free(dx), dev_free(dy), dev_free(dg), dev_free(dp);
+    return SBC_OK;
+}
+
+int sbc_get_roster(sbc_forest* f, int64_t r, int level, int32_t* out, int* n)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "state read: the forest's graph was destroyed");
+    if (!f || !n || r < 0 || r >= f->nk || level < 0 || level >= sbc::kRosterLevels)
+        return fail(SBC_ERR_ARG, "sbc_get_roster: bad arguments");
+    if (!f->d_roster) {
+        *n = -1;
+        return SBC_OK;
+    }
+    if (use_device(f->g->device)) return SBC_ERR_CUDA;
+    CK(cudaStreamSynchronize(f->g->stream));
+    const size_t w = (size_t)r * sbc::kRosterLevels + level;
+    int c = 0;
+    CK(cudaMemcpy(&c, f->d_roster_n + w, sizeof c, cudaMemcpyDeviceToHost));
+    *n = c <= sbc::kRosterCap ? c : -1;
+    if (out && c > 0 && c <= sbc::kRosterCap)
+        CK(cudaMemcpy(out, f->d_roster + w * sbc::kRosterCap, sizeof(int32_t) * c, cudaMemcpyDeviceToHost));
     return SBC_OK;
 }
 

@@ -145,6 +145,8 @@ cudaError_t launch_group_update(sbc_group* G, const int* counts, unsigned steps)
         const int grid = (int)std::min<int64_t>(G->ws.workers, total);
         kGroupVariants[G->variant].launch(A, grid, s);
         if ((e = cudaGetLastError())) return e;
+        for (int i = 0; i < ns; ++i)
+            if ((e = launch_roster_compact(G->members[i], s))) return e;
     }
     if (steps & GROUP_SEAL) return launch_seal_group(B, s);
     return cudaSuccess;

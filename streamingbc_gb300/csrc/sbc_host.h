@@ -180,6 +180,9 @@ struct sbc_forest {
     int64_t workers_req = 0;  // worker count the caller asked for (0 = one per resident CTA)
     int groups = 0;           // groups this forest is a member of
     int32_t* d_lvlhist = nullptr;  // [nk][kHistLevels] vertices per level of each root's tree
+    int32_t* d_roster = nullptr;   // [nk][kRosterLevels][kRosterCap] small-level members (null: no rosters)
+    int32_t* d_roster_n = nullptr;
+    int32_t* d_roster_dirty = nullptr;
     CostModel* model = nullptr;    // allocated by the first cost-model call
     int schedule = 0;              // root order of a batch: 0 static (classify order), 1 cost model
     int64_t state_bytes = 0;
@@ -337,6 +340,9 @@ inline ForestSlot forest_slot(const sbc_forest* f, int n)
     s.nk = (int)f->nk;
     s.lvlhist = f->d_lvlhist;
     s.cost_log = nullptr;
+    s.roster = f->d_roster;
+    s.roster_n = f->d_roster_n;
+    s.roster_dirty = f->d_roster_dirty;
     return s;
 }
 
@@ -358,6 +364,10 @@ cudaError_t launch_seal(sbc_graph* g, int n);
 cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq);
 // Cost model and schedule (sbc_model.cu).
 cudaError_t launch_level_hist(sbc_forest* f);
+// Rosters of every root from its distances (after static init), and the
+// compaction of rosters that hold stale entries (after each batch).
+cudaError_t launch_roster_build(sbc_forest* f);
+cudaError_t launch_roster_compact(sbc_forest* f, cudaStream_t s);
 // Before the update of a batch of n: features of every active (root,
 // insertion) pair into the log buffers (when logging) and, under the model
 // schedule, the worklist ordered by predicted cost (longest first);

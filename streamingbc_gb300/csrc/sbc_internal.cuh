@@ -60,10 +60,21 @@ struct ForestSlot {
     int nk;
     int32_t* lvlhist;   // [nk][kHistLevels] vertices per level (last bucket: that level and deeper), or null
     int32_t* cost_log;  // [nk][nins] touched vertices of each job (cost-model training data), or null
+    int32_t* roster;    // [nk][kRosterLevels][kRosterCap] members of small levels, or null
+    int32_t* roster_n;  // [nk][kRosterLevels] entries (> kRosterCap: level not tracked)
+    int32_t* roster_dirty;  // [nk][kRosterLevels] 1 once an entry went stale
 };
 
 // Levels tracked by the per-root level histograms (deeper levels share the last bucket).
 constexpr int kHistLevels = 64;
+// Rosters: per root, the members of every level 2..kRosterLevels-1 that has at
+// most kRosterCap vertices.  A roster is a superset of its level (entries of
+// vertices that moved to a shallower level stay until compaction; readers
+// check the distance), so a vertex deep in the tree can find its parents
+// among the few members of the level above by binary search in its own
+// sorted adjacency instead of scanning that adjacency.
+constexpr int kRosterLevels = 16;
+constexpr int kRosterCap = 256;
 
 struct Scratch {
     int32_t* st;

@@ -81,7 +81,7 @@ struct FeatArgs {
 
 // Features of insertion i for root r, endpoints ordered a (shallower), b:
 //   d(r,a), d(r,b) (64 if unreachable), level difference (64 if b unreachable),
-//   log1p deg(a), log1p deg(b), log1p sigma(r,a), log1p sigma(r,b),
+//   log1p deg(a), log1p deg(b), log1p |sigma(r,a)|, log1p |sigma(r,b)|,
 //   log1p(vertices at level d(r,a)+1, where the descent from b starts).
 // Returns false if the pair needs no job (insertion not live, or same level).
 __device__ __forceinline__ bool pair_features(const FeatArgs& A, int r, int i, float f[kIn])
@@ -100,8 +100,10 @@ __device__ __forceinline__ bool pair_features(const FeatArgs& A, int r, int i, f
     f[2] = db == SBC_INF ? 64.f : (float)min(db - da, 63);
     f[3] = log1pf((float)A.deg0[a]);
     f[4] = log1pf((float)A.deg0[b]);
-    f[5] = log1pf((float)S[a]);
-    f[6] = db == SBC_INF ? 0.f : log1pf((float)S[b]);
+    // sigma is int64 with wrap-around (as in the reference); a wrapped count
+    // is negative, so its magnitude is taken to keep the feature finite
+    f[5] = log1pf(fabsf((float)S[a]));
+    f[6] = db == SBC_INF ? 0.f : log1pf(fabsf((float)S[b]));
     f[7] = log1pf((float)H[min(da + 1, kHistLevels - 1)]);
     return true;
 }

@@ -171,7 +171,8 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     kVariants[f->variant].launch(A, grid, s);
     f->prof_end(PROF_UPDATE);
     if ((e = cudaGetLastError())) return e;
-    return launch_log_append(f, n);
+    if ((e = launch_log_append(f, n))) return e;
+    return launch_roster_compact(f, s);
 }
 
 }  // namespace sbc

@@ -91,11 +91,22 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
             const int s = W.st[k];
             const int nl = Lb + (s & SBC_STEP_MASK) - 1;
             if (D[k] != nl) {
+                const int old = D[k];
                 if (A.lvlhist) {
                     int32_t* H = A.lvlhist + (size_t)r * kHistLevels;
-                    const int old = D[k];
                     if (old != SBC_INF) atomicSub(&H[min(old, kHistLevels - 1)], 1);
                     atomicAdd(&H[min(nl, kHistLevels - 1)], 1);
+                }
+                if (A.roster) {
+                    // k joins level nl's roster (if tracked); its entry in the
+                    // roster of its old level goes stale
+                    const size_t rb = (size_t)r * kRosterLevels;
+                    if (nl >= 2 && nl < kRosterLevels && A.roster_n[rb + nl] <= kRosterCap) {
+                        const int p = atomicAdd(&A.roster_n[rb + nl], 1);
+                        if (p < kRosterCap) A.roster[(rb + nl) * kRosterCap + p] = k;
+                    }
+                    if (old >= 2 && old < kRosterLevels && A.roster_n[rb + old] <= kRosterCap)
+                        A.roster_dirty[rb + old] = 1;
                 }
                 D[k] = nl;
                 D8[k] = enc_d8(nl);
@@ -202,12 +213,14 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
     };
     long long pull2_cost = -1;  // scanned slots of a level-2 pull (root's neighbours), computed once
 
-    // Level-2 parents of each listed (committed) vertex x: every root
-    // neighbour y (all at level 1) is looked up in x's sorted adjacency; a hit
-    // is a parent, which receives x's child weight (wn[x] if y is in the
-    // descent or (y,x) = (a,b), else wd[x]) and is claimed.  Warp per x, lanes
-    // over y.
-    auto probe_parents = [&](const int32_t* list, int n, int64_t rrow, int rdeg) {
+    // Parents of each listed (committed) vertex x at level L, found among
+    // candidates cand[0..ncand) -- the root's neighbours (all at level 1) for
+    // L = 2, else the roster of level L-1 (entries whose one-byte distance is
+    // not L-1 are stale and skipped): each candidate y is looked up in x's
+    // sorted adjacency; a hit is a parent, which receives x's child weight
+    // (wn[x] if y is in the descent or (y,x) = (a,b), else wd[x]) and is
+    // claimed.  Warp per x, lanes over the candidates.
+    auto probe_parents = [&](const int32_t* list, int n, const int32_t* cand, int ncand, bool check) {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         unsigned cost = 0;
         for (int i = warp; i < n; i += NT / 32) {
@@ -216,8 +229,9 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
             const int vx = vis_deg(A.G, x, rx, g);
             const double wn = W.acc[x];
             const double wd = __longlong_as_double((long long)W.dp[x]);
-            for (int t = lane; t < rdeg; t += 32) {
-                const int y = A.G.col[rrow + t];
+            for (int t = lane; t < ncand; t += 32) {
+                const int y = cand[t];
+                if (check && D8[y] != L - 1) continue;
                 if (!has_edge(A.G, x, rx, vx, y, cost)) continue;
                 const int sy = W.st[y];
                 const bool yDown = (sy & SBC_STEP_MASK) != 0;
@@ -232,6 +246,30 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
         __syncthreads();
     };
 
+    // Levels L >= 3 whose level L-1 has a roster: a vertex whose adjacency is
+    // much longer than the roster is committed as usual but left out of the
+    // walk's scan (its degree is zeroed) and listed at the tail of the level
+    // offsets array instead; the probe pass then finds its parents among the
+    // roster.  The reference edge counter still counts its full degree.
+    const int32_t* rcand = nullptr;
+    int rcnt = 0;
+    auto prep_div = [&](int j, int x, int& d) {
+        prep(j, x, d);
+        if (rcand && (long long)d > (long long)kProbeRatio * rcnt) {
+            W.acc[x] = sm.wn[j];
+            W.dp[x] = (int64_t)__double_as_longlong(sm.wd[j]);
+            W.lvl[nv + 1 - atomicAdd(&sm.nprobe, 1)] = x;
+            atomicAdd(&sm.lb.walked_e, (unsigned long long)d);
+            d = 0;
+        }
+    };
+    auto probe_diverted = [&]() {
+        const int n = sm.nprobe;
+        __syncthreads();
+        if (threadIdx.x == 0) sm.nprobe = 0;
+        if (n > 0) probe_parents(W.lvl + nv + 2 - n, n, rcand, rcnt, true);
+    };
+
     int ua_lo = 0, ua_hi = 0;
     const int Lmax = Lb + nsteps - 1;
     for (L = Lmax; L >= 0; --L) {
@@ -244,6 +282,16 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
         }
         const int next_lo = sm.at;
         const bool pull_ok = L >= 1 && L <= 2 && (!moving || L < Lb);
+        rcand = nullptr;
+        rcnt = 0;
+        if (A.roster && L >= 3 && L - 1 < kRosterLevels) {
+            const size_t rb = (size_t)r * kRosterLevels + (L - 1);
+            const int c = A.roster_n[rb];
+            if (c > 0 && c <= kRosterCap) {
+                rcand = A.roster + rb * kRosterCap;
+                rcnt = c;
+            }
+        }
         if (L == 0) {
             // The root alone (if reached): no parents, committing is all.
             if (threadIdx.x == 0 && dn + ua_hi - ua_lo > 0) {
@@ -322,7 +370,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                     const int nscan = sm.nscan, nprobe = sm.nprobe;
                     lb_walk<NT, false>(A.G, g, D, D8, W.qs + qbase, nscan, nullptr, 0, sm.lb, prep_loaded,
                                        [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
-                    probe_parents(W.qs + nv - nprobe, nprobe, rrow, rdeg);
+                    probe_parents(W.qs + nv - nprobe, nprobe, A.G.col + rrow, rdeg, false);
                 }
                 for (int i = threadIdx.x; i < dn + na_; i += NT) {
                     const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
@@ -331,8 +379,9 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 __syncthreads();
             }
         } else if (!moving) {
-            lb_walk<NT>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep,
+            lb_walk<NT>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep_div,
                         [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+            probe_diverted();
         } else {
             const int same_lo = sm.st;
             lb_walk<NT>(
@@ -355,7 +404,8 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 NoPost());
             const int same_hi = sm.st;
             lb_walk<NT>(A.G, g, D, D8, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
-                        prep, [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+                        prep_div, [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+            probe_diverted();
         }
         ua_lo = next_lo;
         ua_hi = sm.at;
@@ -379,6 +429,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
     for (int i = threadIdx.x; i < ns; i += NT) {
         const int k = W.qs[i];
         W.st[k] = 0;
+        W.dp[k] = 0;  // may hold a child weight (probed levels)
         W.acc[k] = 0.0;
     }
     __syncthreads();

@@ -129,6 +129,7 @@ def load(path: str = LIB_PATH):
         "sbc_cost_model_predict": (C.c_int, [_vp, C.c_int64, _f32p, _f32p]),
         "sbc_cost_model_grad": (C.c_int, [_vp, C.c_int64, _f32p, _f32p, _f32p, _f32p]),
         "sbc_get_level_hist": (C.c_int, [_vp, C.c_int64, C.c_int64, _i32p]),
+        "sbc_get_roster": (C.c_int, [_vp, C.c_int64, C.c_int, _i32p, C.POINTER(C.c_int)]),
         "sbc_insert_batch_async": (C.c_int, [_vp, C.c_int64, _i64p, _i64p]),
         "sbc_server_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.c_int64, C.c_int]),
         "sbc_server_destroy": (C.c_int, [_vp]),
@@ -354,6 +355,13 @@ class DeviceForest:
         _check(self.lib.sbc_cost_model_grad(self.h, len(x), x.ctypes.data_as(_f32p), y.ctypes.data_as(_f32p),
                                             g.ctypes.data_as(_f32p), pred.ctypes.data_as(_f32p)))
         return g, pred
+
+    def roster(self, r: int, level: int):
+        """Members listed for level `level` of root row r, or None if untracked."""
+        out = np.zeros(256, dtype=np.int32)
+        n = C.c_int(0)
+        _check(self.lib.sbc_get_roster(self.h, int(r), int(level), out.ctypes.data_as(_i32p), C.byref(n)))
+        return None if n.value < 0 else out[:n.value].copy()
 
     def level_hist(self) -> np.ndarray:
         out = np.zeros((self.nk, 64), dtype=np.int32)

@@ -144,7 +144,8 @@ def test_logging_training_and_model_schedule(sbc_lib):
         st = fA.insert(ins[s:s + 64])
         fB.insert(ins[s:s + 64])
         n = fA.cost_log_stop()
-        _, y = fA.cost_log_read(seen, n - seen)
+        x, y = fA.cost_log_read(seen, n - seen)
+        assert np.isfinite(x).all() and np.isfinite(y).all()
         touched = np.rint(np.expm1(y.astype(np.float64))).sum()
         assert touched == st["vertices"], (s, touched, st["vertices"])
         seen = n

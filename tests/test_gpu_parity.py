@@ -383,3 +383,38 @@ def test_switching_shapes_between_batches(sbc_lib, port_lib):
         check_state(f, o.level(), o.sigma(), o.bc())
     f.close()
     dg.close()
+
+
+def test_rosters_on_deep_trees(sbc_lib, port_lib):
+    """Roots of degree 1 in an R-MAT graph have deep trees whose hubs sit below
+    small levels; their parents are found through the rosters of those levels.
+    State equals the oracle after every batch, and every tracked roster holds
+    exactly its level's members."""
+    g = G.rmat(12, 8, seed=41)
+    deg = np.diff(g.off)
+    leaves = np.nonzero(deg == 1)[0]
+    rng = np.random.default_rng(41)
+    roots = np.unique(np.concatenate([rng.choice(leaves, 24, replace=False),
+                                      G.pick_roots(g.nv, 8, seed=41)]))
+    ins = G.rmat_insertions(g, 12, 256, seed=41)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    tracked = 0
+    for s in range(0, len(ins), 32):
+        for u, v in ins[s:s + 32]:
+            o.insert(int(u), int(v))
+        f.insert(ins[s:s + 32])
+        check_state(f, o.level(), o.sigma(), o.bc())
+        d = f.dist()
+        for r in range(len(roots)):
+            for lv in range(2, 16):
+                ros = f.roster(r, lv)
+                if ros is None:
+                    continue
+                tracked += 1
+                assert sorted(ros.tolist()) == np.nonzero(d[r] == lv)[0].tolist(), (r, lv)
+    assert tracked > 0
+    f.close()
+    dg.close()
