@@ -56,7 +56,7 @@ __global__ void k_classify_group(const __grid_constant__ GroupUpdateArgs A)
     if (active) A.worklist[atomicAdd(A.nwork, 1)] = ((uint32_t)lo << kSlotShift) | (uint32_t)r;
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, int ILP>
 __global__ void __launch_bounds__(NT, MINB) k_update_group(const __grid_constant__ GroupUpdateArgs A)
 {
     __shared__ UpdSmem<NT> sm;
@@ -71,43 +71,48 @@ __global__ void __launch_bounds__(NT, MINB) k_update_group(const __grid_constant
         __syncthreads();
         if (item >= nwork) break;
         const uint32_t e = A.worklist[item];
-        process_root<NT>(A.slot[e >> kSlotShift], sm, W, (int)(e & kRootMask), false, c1, c2);
+        process_root<NT, ILP>(A.slot[e >> kSlotShift], sm, W, (int)(e & kRootMask), false, c1, c2);
     }
     flush_counters<NT>(sm, A.counters, c1, c2);
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, int ILP>
 void launch_group_variant(const GroupUpdateArgs& A, int grid, cudaStream_t s)
 {
-    k_update_group<NT, MINB><<<grid, NT, 0, s>>>(A);
+    k_update_group<NT, MINB, ILP><<<grid, NT, 0, s>>>(A);
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, int ILP>
 int occupancy_group_variant()
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_update_group<NT, MINB>, NT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_update_group<NT, MINB, ILP>, NT, 0);
     return n;
 }
 
 struct GroupVariant {
-    int threads, min_blocks;
+    int threads, min_blocks, ilp;
     void (*launch)(const GroupUpdateArgs&, int, cudaStream_t);
     int (*occupancy)();
 };
 
 // Same shapes, in the same order, as the single-forest update kernel's table.
 static const GroupVariant kGroupVariants[] = {
-    {256, 4, launch_group_variant<256, 4>, occupancy_group_variant<256, 4>},
-    {256, 5, launch_group_variant<256, 5>, occupancy_group_variant<256, 5>},
-    {256, 6, launch_group_variant<256, 6>, occupancy_group_variant<256, 6>},
-    {128, 8, launch_group_variant<128, 8>, occupancy_group_variant<128, 8>},
-    {128, 10, launch_group_variant<128, 10>, occupancy_group_variant<128, 10>},
-    {512, 2, launch_group_variant<512, 2>, occupancy_group_variant<512, 2>},
-    {512, 1, launch_group_variant<512, 1>, occupancy_group_variant<512, 1>},
-    {1024, 1, launch_group_variant<1024, 1>, occupancy_group_variant<1024, 1>},
-    {64, 16, launch_group_variant<64, 16>, occupancy_group_variant<64, 16>},
-    {32, 32, launch_group_variant<32, 32>, occupancy_group_variant<32, 32>},
+    {256, 4, 4, launch_group_variant<256, 4, 4>, occupancy_group_variant<256, 4, 4>},
+    {256, 5, 4, launch_group_variant<256, 5, 4>, occupancy_group_variant<256, 5, 4>},
+    {256, 6, 4, launch_group_variant<256, 6, 4>, occupancy_group_variant<256, 6, 4>},
+    {128, 8, 4, launch_group_variant<128, 8, 4>, occupancy_group_variant<128, 8, 4>},
+    {128, 10, 4, launch_group_variant<128, 10, 4>, occupancy_group_variant<128, 10, 4>},
+    {512, 2, 4, launch_group_variant<512, 2, 4>, occupancy_group_variant<512, 2, 4>},
+    {512, 1, 4, launch_group_variant<512, 1, 4>, occupancy_group_variant<512, 1, 4>},
+    {1024, 1, 4, launch_group_variant<1024, 1, 4>, occupancy_group_variant<1024, 1, 4>},
+    {64, 16, 4, launch_group_variant<64, 16, 4>, occupancy_group_variant<64, 16, 4>},
+    {32, 32, 4, launch_group_variant<32, 32, 4>, occupancy_group_variant<32, 32, 4>},
+    // deeper (8) or shallower (2) gather pipelines per thread
+    {1024, 1, 8, launch_group_variant<1024, 1, 8>, occupancy_group_variant<1024, 1, 8>},
+    {512, 2, 8, launch_group_variant<512, 2, 8>, occupancy_group_variant<512, 2, 8>},
+    {128, 8, 2, launch_group_variant<128, 8, 2>, occupancy_group_variant<128, 8, 2>},
+    {256, 4, 2, launch_group_variant<256, 4, 2>, occupancy_group_variant<256, 4, 2>},
 };
 constexpr int kNumGroupVariants = sizeof(kGroupVariants) / sizeof(kGroupVariants[0]);
 

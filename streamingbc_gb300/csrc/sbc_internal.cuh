@@ -203,7 +203,7 @@ struct LbSmem {
 
 // Edges each thread has in flight per round of the walker: the adjacency
 // slots of all of them are loaded first, then all neighbour-distance gathers,
-// and only then are they processed, so a thread keeps kEdgeIlp independent
+// and only then are they processed, so a thread keeps ILP (default kEdgeIlp) independent
 // HBM reads outstanding instead of one.
 constexpr int kEdgeIlp = 4;
 
@@ -217,7 +217,7 @@ constexpr int kEdgeIlp = 4;
 // >= 254).  post(j, x) runs after the chunk's edges.  Ends with a barrier.
 // REF: the walked vertices and their degrees count as traversed in the
 // reference's sense (COUNT_TRAVERSALS); every walk counts its scanned slots.
-template <int NT, bool REF = true, class Prep, class Edge, class Post>
+template <int NT, bool REF = true, int ILP = kEdgeIlp, class Prep, class Edge, class Post>
 __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t* D, const uint8_t* D8,
                                         const int32_t* l1, int n1, const int32_t* l2, int n2, LbSmem<NT>& sm,
                                         Prep prep, Edge edge, Post post)
@@ -249,10 +249,10 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t*
         }
         __syncthreads();
         int j = 0;  // chunk vertex of this thread's current edge; edges only move forward
-        for (int e0 = t; e0 < total; e0 += NT * kEdgeIlp) {
-            int kk[kEdgeIlp], jj[kEdgeIlp], dk[kEdgeIlp];
+        for (int e0 = t; e0 < total; e0 += NT * ILP) {
+            int kk[ILP], jj[ILP], dk[ILP];
 #pragma unroll
-            for (int u = 0; u < kEdgeIlp; ++u) {
+            for (int u = 0; u < ILP; ++u) {
                 const int e = e0 + u * NT;
                 kk[u] = -1;
                 jj[u] = j;
@@ -271,14 +271,14 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t*
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kEdgeIlp; ++u) dk[u] = kk[u] >= 0 ? (int)D8[kk[u]] : 0;
+            for (int u = 0; u < ILP; ++u) dk[u] = kk[u] >= 0 ? (int)D8[kk[u]] : 0;
 #pragma unroll
-            for (int u = 0; u < kEdgeIlp; ++u) {
+            for (int u = 0; u < ILP; ++u) {
                 if (dk[u] == SBC_D8_INF) dk[u] = SBC_INF;
                 else if (dk[u] == SBC_D8_DEEP) dk[u] = D[kk[u]];
             }
 #pragma unroll
-            for (int u = 0; u < kEdgeIlp; ++u)
+            for (int u = 0; u < ILP; ++u)
                 if (kk[u] >= 0) edge(jj[u], sm.x[jj[u]], kk[u], dk[u]);
         }
         __syncthreads();
@@ -303,7 +303,7 @@ struct NoPost {
 // GATHER = false skips the distance gather (contrib then receives 0), for
 // walks whose edge test needs no distance.
 constexpr int kSumHit = 4;
-template <int NT, bool GATHER, class Prep, class Contrib, class Post>
+template <int NT, bool GATHER, int ILP = kEdgeIlp, class Prep, class Contrib, class Post>
 __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const int32_t* D, const uint8_t* D8,
                                             const int32_t* l1, int n1, LbSmem<NT>& sm, double* s_sum, int* s_hit,
                                             Prep prep, Contrib contrib, Post post)
@@ -332,10 +332,10 @@ __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const int3
         int j = 0;
         int cj = -1;       // source vertex of the running sum
         double cs = 0.0;   // running sum
-        for (int e0 = t; e0 < total; e0 += NT * kEdgeIlp) {
-            int kk[kEdgeIlp], jj[kEdgeIlp], dk[kEdgeIlp];
+        for (int e0 = t; e0 < total; e0 += NT * ILP) {
+            int kk[ILP], jj[ILP], dk[ILP];
 #pragma unroll
-            for (int u = 0; u < kEdgeIlp; ++u) {
+            for (int u = 0; u < ILP; ++u) {
                 const int e = e0 + u * NT;
                 kk[u] = -1;
                 jj[u] = j;
@@ -354,16 +354,16 @@ __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const int3
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kEdgeIlp; ++u) dk[u] = (GATHER && kk[u] >= 0) ? (int)D8[kk[u]] : 0;
+            for (int u = 0; u < ILP; ++u) dk[u] = (GATHER && kk[u] >= 0) ? (int)D8[kk[u]] : 0;
             if (GATHER) {
 #pragma unroll
-                for (int u = 0; u < kEdgeIlp; ++u) {
+                for (int u = 0; u < ILP; ++u) {
                     if (dk[u] == SBC_D8_INF) dk[u] = SBC_INF;
                     else if (dk[u] == SBC_D8_DEEP) dk[u] = D[kk[u]];
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kEdgeIlp; ++u) {
+            for (int u = 0; u < ILP; ++u) {
                 double v;
                 if (kk[u] >= 0 && contrib(jj[u], sm.x[jj[u]], kk[u], dk[u], v)) {
                     if (jj[u] != cj) {

@@ -49,7 +49,7 @@ struct UpdateArgs {
     unsigned long long* counters;  // vertices, edges, case1, case2, scanned
 };
 
-template <int NT, int MINB>
+template <int NT, int MINB, int ILP>
 __global__ void __launch_bounds__(NT, MINB) k_update(const __grid_constant__ UpdateArgs A)
 {
     __shared__ UpdSmem<NT> sm;
@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(NT, MINB) k_update(const __grid_constant__ Upd
         const int item = sm.item;
         __syncthreads();
         if (item >= nwork) break;
-        process_root<NT>(A.f, sm, W, A.worklist[item], A.all_visible != 0, c1, c2);
+        process_root<NT, ILP>(A.f, sm, W, A.worklist[item], A.all_visible != 0, c1, c2);
     }
     flush_counters<NT>(sm, A.counters, c1, c2);
 }
@@ -89,39 +89,44 @@ __global__ void k_classify(const int32_t* __restrict__ dist, int64_t nv, int nk,
 // of resident CTAs per SM the compiler must fit (which caps registers).  More
 // resident CTAs means more roots in flight and more outstanding gathers; more
 // threads per CTA means faster walks over one root's frontiers.
-template <int NT, int MINB>
+template <int NT, int MINB, int ILP>
 void launch_variant(const UpdateArgs& A, int grid, cudaStream_t s)
 {
-    k_update<NT, MINB><<<grid, NT, 0, s>>>(A);
+    k_update<NT, MINB, ILP><<<grid, NT, 0, s>>>(A);
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, int ILP>
 int occupancy_variant()
 {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_update<NT, MINB>, NT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_update<NT, MINB, ILP>, NT, 0);
     return n;
 }
 
 struct UpdateVariant {
-    int threads, min_blocks;
+    int threads, min_blocks, ilp;
     void (*launch)(const UpdateArgs&, int, cudaStream_t);
     int (*occupancy)();
 };
 
 static const UpdateVariant kVariants[] = {
-    {256, 4, launch_variant<256, 4>, occupancy_variant<256, 4>},
-    {256, 5, launch_variant<256, 5>, occupancy_variant<256, 5>},
-    {256, 6, launch_variant<256, 6>, occupancy_variant<256, 6>},
-    {128, 8, launch_variant<128, 8>, occupancy_variant<128, 8>},
-    {128, 10, launch_variant<128, 10>, occupancy_variant<128, 10>},
-    {512, 2, launch_variant<512, 2>, occupancy_variant<512, 2>},
-    {512, 1, launch_variant<512, 1>, occupancy_variant<512, 1>},
-    {1024, 1, launch_variant<1024, 1>, occupancy_variant<1024, 1>},
+    {256, 4, 4, launch_variant<256, 4, 4>, occupancy_variant<256, 4, 4>},
+    {256, 5, 4, launch_variant<256, 5, 4>, occupancy_variant<256, 5, 4>},
+    {256, 6, 4, launch_variant<256, 6, 4>, occupancy_variant<256, 6, 4>},
+    {128, 8, 4, launch_variant<128, 8, 4>, occupancy_variant<128, 8, 4>},
+    {128, 10, 4, launch_variant<128, 10, 4>, occupancy_variant<128, 10, 4>},
+    {512, 2, 4, launch_variant<512, 2, 4>, occupancy_variant<512, 2, 4>},
+    {512, 1, 4, launch_variant<512, 1, 4>, occupancy_variant<512, 1, 4>},
+    {1024, 1, 4, launch_variant<1024, 1, 4>, occupancy_variant<1024, 1, 4>},
     // one or two warps per root (coarse grain): many roots in flight, for
     // graphs whose per-root touched sets are a few hundred vertices
-    {64, 16, launch_variant<64, 16>, occupancy_variant<64, 16>},
-    {32, 32, launch_variant<32, 32>, occupancy_variant<32, 32>},
+    {64, 16, 4, launch_variant<64, 16, 4>, occupancy_variant<64, 16, 4>},
+    {32, 32, 4, launch_variant<32, 32, 4>, occupancy_variant<32, 32, 4>},
+    // deeper (8) or shallower (2) gather pipelines per thread
+    {1024, 1, 8, launch_variant<1024, 1, 8>, occupancy_variant<1024, 1, 8>},
+    {512, 2, 8, launch_variant<512, 2, 8>, occupancy_variant<512, 2, 8>},
+    {128, 8, 2, launch_variant<128, 8, 2>, occupancy_variant<128, 8, 2>},
+    {256, 4, 2, launch_variant<256, 4, 2>, occupancy_variant<256, 4, 2>},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 // 1024 threads x 1 CTA per SM measured fastest on R-MAT scale 20, K = 1024

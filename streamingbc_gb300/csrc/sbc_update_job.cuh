@@ -25,7 +25,7 @@ struct UpdSmem {
 // many times the root's degree; a probe is costed as this many scanned slots.
 constexpr int kProbeRatio = 32;
 
-template <int NT>
+template <int NT, int ILP>
 __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r,
                                         int a, int b, bool moving, int g)
 {
@@ -56,7 +56,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
     while (lo < hi) {
         const int L = Lb + step;
         const int tag = step + 2;
-        lb_walk<NT>(
+        lb_walk<NT, true, ILP>(
             A.G, g, D, D8, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
             [&](int j, int x, int d) { sm.dp[j] = W.dp[x]; },
             [&](int j, int x, int k, int dk) {
@@ -185,7 +185,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
     // candidate parent tests a neighbour with one (L2-resident) bit instead of
     // gathering its distance and state.
     auto pull_walk = [&](const int32_t* plist, int pn) {
-        lb_walk_sum<NT, false>(
+        lb_walk_sum<NT, false, ILP>(
             A.G, g, D, D8, plist, pn, sm.lb, sm.wn, sm.fl,
             [&](int j, int y, int d) {
                 const int sy = W.st[y];
@@ -368,7 +368,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                     pull_walk(A.G.col + rrow, rdeg);
                 } else {
                     const int nscan = sm.nscan, nprobe = sm.nprobe;
-                    lb_walk<NT, false>(A.G, g, D, D8, W.qs + qbase, nscan, nullptr, 0, sm.lb, prep_loaded,
+                    lb_walk<NT, false, ILP>(A.G, g, D, D8, W.qs + qbase, nscan, nullptr, 0, sm.lb, prep_loaded,
                                        [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
                     probe_parents(W.qs + nv - nprobe, nprobe, A.G.col + rrow, rdeg, false);
                 }
@@ -379,12 +379,12 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 __syncthreads();
             }
         } else if (!moving) {
-            lb_walk<NT>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep_div,
+            lb_walk<NT, true, ILP>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep_div,
                         [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
             probe_diverted();
         } else {
             const int same_lo = sm.st;
-            lb_walk<NT>(
+            lb_walk<NT, true, ILP>(
                 A.G, g, D, D8, dlist, dn, nullptr, 0, sm.lb, prep,
                 [&](int j, int x, int k, int dk) {
                     if (parent_edge(j, x, k, dk)) return;
@@ -403,7 +403,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 },
                 NoPost());
             const int same_hi = sm.st;
-            lb_walk<NT>(A.G, g, D, D8, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
+            lb_walk<NT, true, ILP>(A.G, g, D, D8, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
                         prep_div, [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
             probe_diverted();
         }
@@ -438,7 +438,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
 // Applies the batch's insertions in order to root r of slot A: each live
 // insertion (append code > 0) whose endpoints sit on different levels is one
 // job, |d| == 1 (case 1) or |d| > 1 / one endpoint unreachable (case 2).
-template <int NT>
+template <int NT, int ILP>
 __device__ __forceinline__ void process_root(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r,
                                              bool all_visible, unsigned long long& c1, unsigned long long& c2)
 {
@@ -457,7 +457,7 @@ __device__ __forceinline__ void process_root(const ForestSlot& A, UpdSmem<NT>& s
             else c1++;
         }
         const unsigned long long walked0 = sm.lb.walked_v;  // read before run_job's first barrier
-        run_job<NT>(A, sm, W, r, a, b, moving, all_visible ? INT_MAX : i);
+        run_job<NT, ILP>(A, sm, W, r, a, b, moving, all_visible ? INT_MAX : i);
         if (A.cost_log && threadIdx.x == 0)
             A.cost_log[(size_t)r * A.nins + i] = (int32_t)min(sm.lb.walked_v - walked0, (unsigned long long)INT_MAX);
     }
