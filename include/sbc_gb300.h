@@ -31,7 +31,7 @@ extern "C" {
 #define SBC_ERR_CUDA (-2)        /* CUDA runtime error (message in sbc_last_error) */
 #define SBC_ERR_NOMEM (-3)       /* device or host allocation failed */
 #define SBC_ERR_STATE (-4)       /* call out of order (e.g. insert before static init) */
-#define SBC_ERR_UNSUPPORTED (-5) /* operation not provided (edge deletion) */
+#define SBC_ERR_UNSUPPORTED (-5) /* operation not provided (vertex deletion) */
 #define SBC_ERR_NOGPU (-6)       /* no CUDA device */
 
 typedef struct sbc_graph sbc_graph;
@@ -311,6 +311,29 @@ int sbc_server_release(sbc_server *s, int id);
  * dist[nk][nv], sigma[nk][nv], bc[nv]. */
 int sbc_server_read(sbc_server *s, int id, int32_t *dist, int64_t *sigma, double *bc);
 int sbc_server_get_stats(sbc_server *s, sbc_server_stats *stats, int reset);
+
+/* ---- edge deletion --------------------------------------------------------
+ * Replaces deleteEdgeStreamingBC (src/streamingbc.c:258-416): per root, the
+ * endpoints on one level (or both unreachable) change nothing; otherwise the
+ * deeper endpoint b either keeps a parent -- sigma-only decrease and
+ * dependency ascent, the reference's removeEdgeWithoutMovementBrandes
+ * (src/streamingbc_internal.c:607-868) -- or loses its last one, and the root
+ * is recomputed from scratch (BC moved by its new minus old dependencies)
+ * instead of the reference's moveDownTreeBrandes (:880-1401), whose results
+ * disagree with a recomputation of the modified graph.  Results equal a
+ * static recompute of the modified graph (tested).  stats->inserted counts
+ * edges removed, duplicates edges absent, invalid bad ids; case1/case2 the
+ * incremental / recomputed (root, deletion) pairs. */
+/* Remove n undirected edges from the graph one at a time, each followed by
+ * the update of every root.  Synchronous; stats may be NULL. */
+int sbc_delete_batch(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, sbc_batch_stats *stats);
+/* The update for one deletion whose edge the caller has already removed in
+ * both directions (sbc_graph_remove_directed x2, or stinger_remove_edge x2),
+ * exactly like deleteEdgeStreamingBC after the caller's removals. */
+int sbc_update_deleted(sbc_forest *f, int64_t u, int64_t v, sbc_batch_stats *stats);
+/* Directed removal with stinger_remove_edge's result: 1 removed, 0 absent,
+ * -1 self loop / bad id.  Synchronous. */
+int sbc_graph_remove_directed(sbc_graph *g, int64_t from, int64_t to, int *result);
 
 /* Wait for all work queued on the forest's graph stream. */
 int sbc_sync(sbc_forest *f);

@@ -47,6 +47,8 @@ def _port_lib():
         lib.orc_graph_free.argtypes = [C.c_void_p]
         lib.orc_graph_insert.restype = C.c_int
         lib.orc_graph_insert.argtypes = [C.c_void_p, C.c_int64, C.c_int64]
+        lib.orc_graph_remove.restype = C.c_int
+        lib.orc_graph_remove.argtypes = [C.c_void_p, C.c_int64, C.c_int64]
         lib.orc_graph_degree.restype = C.c_int64
         lib.orc_graph_degree.argtypes = [C.c_void_p, C.c_int64]
         lib.orc_forest_new.restype = C.c_void_p
@@ -112,6 +114,19 @@ class PortOracle:
         self.lib.orc_graph_insert(self.g, int(v), int(u))
         self.lib.orc_insert(self.f, self.g, int(u), int(v))
 
+    def delete(self, u: int, v: int) -> bool:
+        """Remove (u,v) from the graph (both directions) and recompute every
+        root from scratch: the state after a deletion, by definition.  (The
+        reference's own deleteEdgeStreamingBC, src/streamingbc.c:258-416,
+        disagrees with this recomputation -- see tests/test_oracle.py -- so
+        deletions are checked against the recomputation.)  Returns whether
+        the edge was present."""
+        a = self.lib.orc_graph_remove(self.g, int(u), int(v))
+        self.lib.orc_graph_remove(self.g, int(v), int(u))
+        if a:
+            self.lib.orc_static(self.f, self.g)
+        return bool(a)
+
     def static_timed(self) -> float:
         return self.lib.orc_static_timed(self.f, self.g)
 
@@ -169,6 +184,8 @@ def _ref_lib():
         lib.ref_static.restype = C.c_double
         lib.ref_insert.restype = C.c_double
         lib.ref_insert.argtypes = [C.c_int64, C.c_int64]
+        lib.ref_delete.restype = C.c_double
+        lib.ref_delete.argtypes = [C.c_int64, C.c_int64]
         lib.ref_counters.argtypes = [_i64p]
         lib.ref_dump.argtypes = [_i64p, _i64p, _f64p, _f64p]
         _ref = lib
@@ -196,6 +213,10 @@ class RefOracle:
 
     def insert(self, u: int, v: int) -> float:
         return self.lib.ref_insert(int(u), int(v))
+
+    def delete(self, u: int, v: int) -> float:
+        """Remove (u,v) from the graph (both directions), then update every root."""
+        return self.lib.ref_delete(int(u), int(v))
 
     def counters(self) -> dict:
         c = np.zeros(4, dtype=np.int64)

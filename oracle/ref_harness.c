@@ -75,6 +75,28 @@ double ref_insert(int64_t u, int64_t v)
     return t;
 }
 
+/* Deletion as the reference's callers do it (src/sbcMain_utils.c:477-484,
+ * :586-591): stinger_remove_edge x2, then deleteEdgeStreamingBC(..., BALANCE,
+ * COARSE) (src/streamingbc.c:258-416).  Counters as for ref_insert (case1 =
+ * adjacent-level deletions, case2 = deletions that move vertices down). */
+double ref_delete(int64_t u, int64_t v)
+{
+    stinger_remove_edge(g_S, 0, u, v);
+    stinger_remove_edge(g_S, 0, v, u);
+    tic();
+    deleteEdgeStreamingBC(g_F, g_S, u, v, g_roots, g_nk, g_nv, g_nt, g_A, BALANCE, COARSE);
+    double t = toc();
+    g_cnt[0] = g_cnt[1] = g_cnt[2] = g_cnt[3] = 0;
+    for (int64_t t2 = 0; t2 < g_nt; t2++) {
+        g_cnt[0] += g_A[t2]->dynamicTraverseVerticeCounter;
+        g_cnt[1] += g_A[t2]->dynamicTraverseEdgeCounter;
+        g_cnt[2] += g_A[t2]->adjacentCounter;
+        g_cnt[3] += g_A[t2]->movementCounter;
+        ClearCounters(g_A[t2]);
+    }
+    return t;
+}
+
 void ref_counters(int64_t *out4) { memcpy(out4, g_cnt, sizeof(g_cnt)); }
 
 void ref_dump(int64_t *level, int64_t *sigma, double *delta, double *bc)

@@ -85,6 +85,20 @@ int64_t orc_graph_degree(const orc_graph *g, int64_t v) { return g->deg[v]; }
 
 /* Directed insert with the return convention of stinger_insert_edge
  * (src/stinger/stinger.c:778-876): -1 self loop, 0 already present, 1 new. */
+/* Remove `to` from the neighbours of `from` (stinger_remove_edge,
+ * src/stinger/stinger.c): 1 removed, 0 absent.  Order of the remaining
+ * neighbours is kept. */
+int orc_graph_remove(orc_graph *g, int64_t from, int64_t to)
+{
+    for (int64_t i = 0; i < g->deg[from]; i++) {
+        if (g->nbr[from][i] != to) continue;
+        for (int64_t j = i + 1; j < g->deg[from]; j++) g->nbr[from][j - 1] = g->nbr[from][j];
+        g->deg[from]--;
+        return 1;
+    }
+    return 0;
+}
+
 int orc_graph_insert(orc_graph *g, int64_t from, int64_t to)
 {
     if (from == to) return -1;

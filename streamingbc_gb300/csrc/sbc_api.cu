@@ -620,7 +620,7 @@ int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int6
         (e = cudaEventCreateWithFlags(&g->staged, cudaEventDisableTiming)) || (e = dev_alloc(&g->d_row, nv + 1)) ||
         (e = dev_alloc(&g->d_deg, nv)) || (e = dev_alloc(&g->d_deg0, nv)) || (e = dev_alloc(&g->d_cap, nv)) ||
         (e = dev_alloc(&g->d_nsort, nv)) ||
-        (e = dev_alloc(&g->d_col, total)) || (e = dev_alloc(&g->d_seq, total)) || (e = dev_alloc(&g->d_err, 1)) ||
+        (e = dev_alloc(&g->d_col, total)) || (e = dev_alloc(&g->d_seq, total)) || (e = dev_alloc(&g->d_err, 2)) ||
         (e = dev_alloc(&g->d_src, 2))) {
         sbc_graph_destroy(g);
         return cuda_fail(e, "sbc_graph_create allocation");
@@ -631,7 +631,7 @@ int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int6
         (nv && (e = cudaMemcpy(g->d_nsort, deg.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
         (nv && (e = cudaMemcpy(g->d_cap, g->h_cap.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
         (e = cudaMemcpy(g->d_col, col.data(), sizeof(int32_t) * col.size(), cudaMemcpyHostToDevice)) ||
-        (e = cudaMemset(g->d_seq, 0, sizeof(int32_t) * col.size())) || (e = cudaMemset(g->d_err, 0, sizeof(int)))) {
+        (e = cudaMemset(g->d_seq, 0, sizeof(int32_t) * col.size())) || (e = cudaMemset(g->d_err, 0, 2 * sizeof(int)))) {
         sbc_graph_destroy(g);
         return cuda_fail(e, "sbc_graph_create upload");
     }
@@ -794,6 +794,7 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
         (e = dev_alloc(&f->d_sigma, cells)) ||
         (e = dev_alloc(&f->d_delta, cells)) || (e = dev_alloc(&f->d_bc, f->nv)) || (e = dev_alloc(&f->d_worklist, nk)) ||
         (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, SBC_NCOUNTERS)) ||
+        (e = dev_alloc(&f->d_mov, nk)) || (e = dev_alloc(&f->d_nmov, 2)) ||
         (e = dev_alloc(&f->d_lvlhist, (size_t)nk * sbc::kHistLevels))) {
         sbc_forest_destroy(f);
         return cuda_fail(e, "sbc_forest_create state allocation");
@@ -846,6 +847,8 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_nwork);
     dev_free(f->d_counters);
     dev_free(f->d_lvlhist);
+    dev_free(f->d_mov);
+    dev_free(f->d_nmov);
     dev_free(f->d_roster);
     dev_free(f->d_roster_n);
     dev_free(f->d_roster_dirty);
@@ -1078,6 +1081,94 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
     CK(sbc::launch_seal(g, (int)n));
     if (chosen) *chosen = best;
     return check_graph_err(g);
+}
+
+// ------------------------------------------------------------------ deletions
+
+int sbc_graph_remove_directed(sbc_graph* g, int64_t from, int64_t to, int* result)
+{
+    if (!g || !result) return fail(SBC_ERR_ARG, "sbc_graph_remove_directed: bad arguments");
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    if (from < 0 || to < 0 || from >= g->nv || to >= g->nv || from == to) {
+        *result = -1;
+        return SBC_OK;
+    }
+    CK(sbc::launch_remove(g, (int)from, (int)to, true, g->d_err + 1));
+    CK(cudaMemcpyAsync(result, g->d_err + 1, sizeof(int), cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    return SBC_OK;
+}
+
+namespace {
+// Deletion statistics of one call from the per-deletion removal codes
+// (staged at d_codes) and the forest's counters.
+int deletion_stats(sbc_forest* f, int64_t n, const int32_t* d_codes, sbc_batch_stats* st)
+{
+    sbc_graph* g = f->g;
+    std::vector<int32_t> codes(n);
+    unsigned long long c[SBC_NCOUNTERS];
+    CK(cudaMemcpyAsync(codes.data(), d_codes, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaMemcpyAsync(c, f->d_counters, sizeof c, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaMemsetAsync(f->d_counters, 0, sizeof c, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    memset(st, 0, sizeof *st);
+    for (int32_t k : codes) {
+        if (k > 0) st->inserted++;
+        else if (k == 0) st->duplicates++;
+        else st->invalid++;
+    }
+    st->vertices = (int64_t)c[0];
+    st->edges = (int64_t)c[1];
+    st->case1 = (int64_t)c[2];
+    st->case2 = (int64_t)c[3];
+    st->scanned = (int64_t)c[4];
+    return SBC_OK;
+}
+}  // namespace
+
+int sbc_delete_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* v, sbc_batch_stats* stats)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_delete_batch: the forest's graph was destroyed");
+    if (!f || n < 0 || (n > 0 && (!u || !v))) return fail(SBC_ERR_ARG, "sbc_delete_batch: bad arguments");
+    if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_delete_batch before sbc_static_init");
+    if (n >= INT32_MAX) return fail(SBC_ERR_ARG, "batch too large");
+    sbc_graph* g = f->g;
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    if (n == 0) {
+        if (stats) memset(stats, 0, sizeof *stats);
+        return SBC_OK;
+    }
+    int rc = ensure_staging(g, n);
+    if (rc) return rc;
+    int32_t* codes = g->d_ins + 2 * g->ins_capacity;
+    if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
+    // one deletion at a time, in order: remove the edge, then update every root
+    for (int64_t i = 0; i < n; ++i) {
+        const bool valid = u[i] >= 0 && v[i] >= 0 && u[i] < g->nv && v[i] < g->nv && u[i] != v[i];
+        const int a = valid ? (int)u[i] : -1, b = valid ? (int)v[i] : -1;
+        CK(sbc::launch_remove(g, a, b, false, codes + i));
+        if (valid) CK(sbc::launch_delete(f, a, b, codes + i));
+    }
+    if (stats) return deletion_stats(f, n, codes, stats);
+    CK(cudaStreamSynchronize(g->stream));
+    return SBC_OK;
+}
+
+int sbc_update_deleted(sbc_forest* f, int64_t u, int64_t v, sbc_batch_stats* stats)
+{
+    if (f && !f->g) return fail(SBC_ERR_STATE, "sbc_update_deleted: the forest's graph was destroyed");
+    if (!f) return fail(SBC_ERR_ARG, "sbc_update_deleted: null");
+    if (!f->initialized) return fail(SBC_ERR_STATE, "sbc_update_deleted before sbc_static_init");
+    sbc_graph* g = f->g;
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    if (u < 0 || v < 0 || u >= g->nv || v >= g->nv || u == v) return fail(SBC_ERR_ARG, "sbc_update_deleted: bad edge");
+    static const int kRemoved = 1;
+    CK(cudaMemcpyAsync(g->d_err + 1, &kRemoved, sizeof(int), cudaMemcpyHostToDevice, g->stream));
+    if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
+    CK(sbc::launch_delete(f, (int)u, (int)v, g->d_err + 1));
+    if (stats) return deletion_stats(f, 1, g->d_err + 1, stats);
+    CK(cudaStreamSynchronize(g->stream));
+    return SBC_OK;
 }
 
 // ------------------------------------------------------------------ cost model
@@ -1796,12 +1887,11 @@ int stinger_insert_edge_pair(struct stinger* G, int64_t type, int64_t from, int6
 
 int stinger_remove_edge(struct stinger* G, int64_t type, int64_t from, int64_t to)
 {
-    (void)G;
     (void)type;
-    (void)from;
-    (void)to;
-    fail(SBC_ERR_UNSUPPORTED, "stinger_remove_edge: edge deletion is not provided");
-    return -1;
+    if (!G || !G->g) return -1;
+    int res = -1;
+    if (sbc_graph_remove_directed(G->g, from, to, &res)) return -1;
+    return res;
 }
 
 int64_t stinger_outdegree(const struct stinger* G, int64_t v)
@@ -1983,10 +2073,30 @@ StreamingExtraInfo deleteEdgeStreamingBC(bcForest* forest, struct stinger* sStin
                                          int64_t* rootArrayForApproximation, int64_t NK, int64_t Nv, int64_t NT,
                                          extraArraysPerThread** eAPT, uint32_t loadBalancing, uint32_t granularity)
 {
-    (void)forest; (void)sStinger; (void)oldU; (void)oldV; (void)rootArrayForApproximation; (void)NK;
-    (void)Nv; (void)NT; (void)eAPT; (void)loadBalancing; (void)granularity;
-    fail(SBC_ERR_UNSUPPORTED, "deleteEdgeStreamingBC: edge deletion is not provided");
+    // The caller has already removed (oldU, oldV) in both directions
+    // (stinger_remove_edge x2, src/sbcMain_utils.c:477-484).
+    (void)rootArrayForApproximation;
+    (void)Nv;
+    (void)NT;
+    (void)loadBalancing;
+    (void)granularity;
     StreamingExtraInfo sei = {0, 0, 0, 0};
+    if (!forest || !forest->sbc || !sStinger || forest->sbc->g != sStinger->g) {
+        fail(SBC_ERR_STATE, "deleteEdgeStreamingBC: static init on this graph has not run");
+        return sei;
+    }
+    sbc_batch_stats st;
+    if (sbc_update_deleted(forest->sbc, oldU, oldV, &st)) return sei;
+    sei.adjacent = st.case1;
+    sei.movement = st.case2;
+    sei.sameLevel = NK - st.case1 - st.case2;
+    if (eAPT && eAPT[0]) {
+        eAPT[0]->adjacentCounter += st.case1;
+        eAPT[0]->movementCounter += st.case2;
+        eAPT[0]->dynamicTraverseVerticeCounter += st.vertices;
+        eAPT[0]->dynamicTraverseEdgeCounter += st.edges;
+    }
+    refresh_bc(forest);
     return sei;
 }
 

@@ -120,6 +120,62 @@ __global__ void k_seal(int n, const int32_t* __restrict__ iu, const int32_t* __r
     deg0[iv[i]] = deg[iv[i]];
 }
 
+// Removes neighbour y from x's slots (one warp): the slot is found, the later
+// slots move down one place (a sorted prefix stays sorted), and deg -- and
+// deg0 / nsort when the slot lay below them -- drop by one.  Returns whether y
+// was present.
+__device__ __forceinline__ bool remove_slot(const int64_t* __restrict__ row, int32_t* deg, int32_t* deg0,
+                                            int32_t* nsort, int32_t* col, int32_t* seq, int x, int y)
+{
+    const int lane = threadIdx.x & 31;
+    const int d = deg[x];
+    const int64_t rx = row[x];
+    int p = -1;
+    for (int base = 0; base < d && p < 0; base += 32) {
+        const int s = base + lane;
+        const unsigned m = __ballot_sync(0xffffffffu, s < d && col[rx + s] == y);
+        if (m) p = base + __ffs(m) - 1;
+    }
+    if (p < 0) return false;
+    for (int base = p; base < d - 1; base += 32) {
+        const int s = base + lane;
+        int c = 0, q = 0;
+        if (s < d - 1) {
+            c = col[rx + s + 1];
+            q = seq[rx + s + 1];
+        }
+        __syncwarp();  // every lane has read before any slot is overwritten
+        if (s < d - 1) {
+            col[rx + s] = c;
+            seq[rx + s] = q;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        deg[x] = d - 1;
+        if (p < deg0[x]) deg0[x] -= 1;
+        if (p < nsort[x]) nsort[x] -= 1;
+    }
+    __syncwarp();
+    return true;
+}
+
+// Edge removal (stinger_remove_edge, src/stinger/stinger.c): (u,v) and,
+// unless directed, (v,u); *res = 1 removed, 0 absent, -1 self loop or id out
+// of range.  One warp; the graph's stream orders it with the batches.
+__global__ void k_remove(int64_t nv, const int64_t* __restrict__ row, int32_t* deg, int32_t* deg0, int32_t* nsort,
+                         int32_t* col, int32_t* seq, int u, int v, int directed, int* res)
+{
+    int code;
+    if (u == v || u < 0 || v < 0 || u >= nv || v >= nv) {
+        code = -1;
+    } else {
+        code = remove_slot(row, deg, deg0, nsort, col, seq, u, v) ? 1 : 0;
+        if (!directed) remove_slot(row, deg, deg0, nsort, col, seq, v, u);
+    }
+    if (threadIdx.x == 0) *res = code;
+}
+
 // k_seal over many graphs: blockIdx.y selects the graph.
 __global__ void k_seal_group(const __grid_constant__ GraphBatchSlots S)
 {
@@ -197,6 +253,13 @@ cudaError_t launch_seal_group(const GraphBatchSlots& S, cudaStream_t s)
     for (int i = 0; i < S.count; ++i) nmax = std::max(nmax, S.slot[i].n);
     if (S.count <= 0 || nmax <= 0) return cudaSuccess;
     k_seal_group<<<dim3((nmax + 255) / 256, S.count), 256, 0, s>>>(S);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_remove(sbc_graph* g, int u, int v, bool directed, int* d_res)
+{
+    k_remove<<<1, 32, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_deg0, g->d_nsort, g->d_col, g->d_seq, u, v,
+                                      directed ? 1 : 0, d_res);
     return cudaGetLastError();
 }
 

@@ -62,8 +62,7 @@ __global__ void __launch_bounds__(NT, MINB) k_update_group(const __grid_constant
     __shared__ UpdSmem<NT> sm;
     const Scratch W = A.scr.of(blockIdx.x, A.scr_nv);
     const int nwork = *A.nwork;
-    unsigned long long c1 = 0, c2 = 0;
-    if (threadIdx.x == 0) sm.lb.walked_v = sm.lb.walked_e = sm.lb.scanned_e = 0;
+    reset_counters<NT>(sm);
     for (;;) {
         if (threadIdx.x == 0) sm.item = atomicAdd(A.work_counter, 1);
         __syncthreads();
@@ -71,9 +70,9 @@ __global__ void __launch_bounds__(NT, MINB) k_update_group(const __grid_constant
         __syncthreads();
         if (item >= nwork) break;
         const uint32_t e = A.worklist[item];
-        process_root<NT, ILP>(A.slot[e >> kSlotShift], sm, W, (int)(e & kRootMask), false, c1, c2);
+        process_root<NT, ILP>(A.slot[e >> kSlotShift], sm, W, (int)(e & kRootMask), false);
     }
-    flush_counters<NT>(sm, A.counters, c1, c2);
+    flush_counters<NT>(sm, A.counters);
 }
 
 template <int NT, int MINB, int ILP>

@@ -188,6 +188,9 @@ struct sbc_forest {
     int64_t state_bytes = 0;
     WorkerScratch ws;
     int* d_worklist = nullptr;
+    int* d_mov = nullptr;     // [nk] roots a deletion leaves without a parent of the deeper endpoint
+    int* d_nmov = nullptr;    // [2]: their count, work counter
+    int* d_res = nullptr;     // [1] result of the last edge removal
     int* d_nwork = nullptr;   // [1]
     int* d_counter = nullptr; // [1]
     // [SBC_NCOUNTERS]: traversed vertices, traversed edges (reference counters),
@@ -362,6 +365,18 @@ cudaError_t launch_set_src(sbc_graph* g, const int32_t* d_u, const int32_t* d_v)
 cudaError_t launch_stage(sbc_graph* g, int n);
 cudaError_t launch_seal(sbc_graph* g, int n);
 cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq);
+// Edge removal (both directions unless directed); *d_res = 1 removed, 0 absent, -1 invalid.
+cudaError_t launch_remove(sbc_graph* g, int u, int v, bool directed, int* d_res);
+// Update for the deletion of (u, v), already removed from the adjacency
+// (*d_removed must be 1, else nothing is done): roots that keep a parent of the
+// deeper endpoint get the sigma-decrease descent and ascent; the others are
+// recomputed from scratch, their old dependencies taken out of BC first.
+cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed);
+// Static recompute of the roots listed (device list and count) or, with a
+// null list, of all roots.
+cudaError_t launch_static_list(sbc_forest* f, const int* d_list, const int* d_nlist);
+cudaError_t launch_level_hist_list(sbc_forest* f, const int* d_list, const int* d_nlist);
+cudaError_t launch_roster_build_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 // Cost model and schedule (sbc_model.cu).
 cudaError_t launch_level_hist(sbc_forest* f);
 // Rosters of every root from its distances (after static init), and the

@@ -194,18 +194,21 @@ __global__ void k_log_append(const float* __restrict__ feat, const int32_t* __re
 
 // Vertices per level (levels from the one-byte shadow; 254 = deep, 255 =
 // unreachable) of every root's tree: CTA per root.
-__global__ void k_level_hist(const uint8_t* __restrict__ dist8, int64_t nv, int32_t* __restrict__ hist)
+__global__ void k_level_hist(const uint8_t* __restrict__ dist8, int64_t nv, int32_t* __restrict__ hist,
+                             const int* __restrict__ list, const int* __restrict__ nlist)
 {
     __shared__ int h[kHistLevels];
+    if (list && (int)blockIdx.x >= *nlist) return;
+    const size_t r = list ? (size_t)list[blockIdx.x] : blockIdx.x;
     for (int t = threadIdx.x; t < kHistLevels; t += blockDim.x) h[t] = 0;
     __syncthreads();
-    const uint8_t* D8 = dist8 + (size_t)blockIdx.x * nv;
+    const uint8_t* D8 = dist8 + r * nv;
     for (int64_t v = threadIdx.x; v < nv; v += blockDim.x) {
         const int d = D8[v];
         if (d != SBC_D8_INF) atomicAdd(&h[min(d, kHistLevels - 1)], 1);
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < kHistLevels; t += blockDim.x) hist[(size_t)blockIdx.x * kHistLevels + t] = h[t];
+    for (int t = threadIdx.x; t < kHistLevels; t += blockDim.x) hist[r * kHistLevels + t] = h[t];
 }
 
 // ---------------------------------------------------------------- training
@@ -408,10 +411,12 @@ __global__ void __launch_bounds__(256) k_predict(const float* __restrict__ param
 
 // ---------------------------------------------------------------- launchers
 
-cudaError_t launch_level_hist(sbc_forest* f)
+cudaError_t launch_level_hist(sbc_forest* f) { return launch_level_hist_list(f, nullptr, nullptr); }
+
+cudaError_t launch_level_hist_list(sbc_forest* f, const int* d_list, const int* d_nlist)
 {
     if (!f->d_lvlhist) return cudaSuccess;
-    k_level_hist<<<(int)f->nk, 256, 0, f->g->stream>>>(f->d_dist8, f->nv, f->d_lvlhist);
+    k_level_hist<<<(int)f->nk, 256, 0, f->g->stream>>>(f->d_dist8, f->nv, f->d_lvlhist, d_list, d_nlist);
     return cudaGetLastError();
 }
 

@@ -25,11 +25,13 @@ namespace sbc {
 
 __global__ void __launch_bounds__(256) k_roster_build(const uint8_t* __restrict__ dist8, int64_t nv,
                                                       const int32_t* __restrict__ hist, int32_t* __restrict__ roster,
-                                                      int32_t* __restrict__ roster_n, int32_t* __restrict__ dirty)
+                                                      int32_t* __restrict__ roster_n, int32_t* __restrict__ dirty,
+                                                      const int* __restrict__ list, const int* __restrict__ nlist)
 {
     __shared__ int cnt[kRosterLevels];
     __shared__ int ok[kRosterLevels];
-    const size_t r = blockIdx.x;
+    if (list && (int)blockIdx.x >= *nlist) return;
+    const size_t r = list ? (size_t)list[blockIdx.x] : blockIdx.x;
     const int32_t* H = hist + r * kHistLevels;
     if (threadIdx.x < kRosterLevels) {
         cnt[threadIdx.x] = 0;
@@ -83,11 +85,13 @@ __global__ void __launch_bounds__(256) k_roster_compact(const uint8_t* __restric
     }
 }
 
-cudaError_t launch_roster_build(sbc_forest* f)
+cudaError_t launch_roster_build(sbc_forest* f) { return launch_roster_build_list(f, nullptr, nullptr); }
+
+cudaError_t launch_roster_build_list(sbc_forest* f, const int* d_list, const int* d_nlist)
 {
     if (!f->d_roster) return cudaSuccess;
     k_roster_build<<<(int)f->nk, 256, 0, f->g->stream>>>(f->d_dist8, f->nv, f->d_lvlhist, f->d_roster,
-                                                          f->d_roster_n, f->d_roster_dirty);
+                                                          f->d_roster_n, f->d_roster_dirty, d_list, d_nlist);
     return cudaGetLastError();
 }
 

@@ -33,6 +33,8 @@ struct StaticArgs {
     ScratchBase scr;
     int* work_counter;
     unsigned long long* counters;  // [0] vertices, [1] edges
+    const int* list;   // roots to (re)compute, or null for all
+    const int* nlist;
 };
 
 template <int NT>
@@ -49,9 +51,10 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(A.work_counter, 1);
         __syncthreads();
-        const int r = s_item;
+        const int item = s_item;
         __syncthreads();
-        if (r >= A.nk) break;
+        if (item >= (A.list ? *A.nlist : A.nk)) break;
+        const int r = A.list ? A.list[item] : item;
         int32_t* D = A.dist + (size_t)r * nv;
         uint8_t* D8 = A.dist8 + (size_t)r * nv;
         int64_t* Sg = A.sigma + (size_t)r * nv;
@@ -154,7 +157,9 @@ int static_workers_per_sm()
     return n;
 }
 
-cudaError_t launch_static(sbc_forest* f)
+cudaError_t launch_static(sbc_forest* f) { return launch_static_list(f, nullptr, nullptr); }
+
+cudaError_t launch_static_list(sbc_forest* f, const int* d_list, const int* d_nlist)
 {
     sbc_graph* g = f->g;
     cudaStream_t s = g->stream;
@@ -172,6 +177,8 @@ cudaError_t launch_static(sbc_forest* f)
     A.scr = f->scratch();
     A.work_counter = f->d_counter;
     A.counters = f->d_counters;
+    A.list = d_list;
+    A.nlist = d_nlist;
     // One worker slot per CTA: with few workers per SM, wider CTAs keep the SMs full.
     const int grid = (int)std::min<int64_t>(f->workers, f->nk);
     const int64_t per_sm = (f->workers + f->sm_count - 1) / f->sm_count;
@@ -181,6 +188,7 @@ cudaError_t launch_static(sbc_forest* f)
     else k_static<256><<<grid, 256, 0, s>>>(A);
     f->prof_end(PROF_STATIC);
     if ((e = cudaGetLastError())) return e;
+    if (d_list) return cudaSuccess;  // the caller moves BC by the listed roots' old and new rows
     int bgrid = (int)std::min<int64_t>((f->nv + 255) / 256, (int64_t)f->sm_count * 8);
     if (bgrid < 1) bgrid = 1;
     k_bc_colsum<<<bgrid, 256, 0, s>>>(f->d_delta, f->d_roots, (int)f->nk, f->nv, f->d_bc);
@@ -312,6 +320,8 @@ extern "C" int sbc_static_init_noalloc(int64_t nv, const int64_t* d_off, const i
     A.scr.acc = (double*)(base + kOffAcc);
     A.work_counter = (int*)(counters + 8);
     A.counters = counters;
+    A.list = nullptr;
+    A.nlist = nullptr;
     k_static<1024><<<slots, 1024, 0, s>>>(A);
     k_bc_colsum<<<dgrid, 256, 0, s>>>(d_delta, d_roots, (int)nk, nv, d_bc);
     if (cudaGetLastError() != cudaSuccess) return noalloc_fail(SBC_ERR_CUDA, "sbc_static_init_noalloc: launch failed");

@@ -43,6 +43,7 @@ struct UpdateArgs {
     ForestSlot f;
     ScratchBase scr;
     int all_visible;
+    int del_u, del_v;  // k_delete: the deleted edge
     const int* worklist;
     const int* nwork;
     int* work_counter;
@@ -55,8 +56,7 @@ __global__ void __launch_bounds__(NT, MINB) k_update(const __grid_constant__ Upd
     __shared__ UpdSmem<NT> sm;
     const Scratch W = A.scr.of(blockIdx.x, A.f.G.nv);
     const int nwork = *A.nwork;
-    unsigned long long c1 = 0, c2 = 0;
-    if (threadIdx.x == 0) sm.lb.walked_v = sm.lb.walked_e = sm.lb.scanned_e = 0;
+    reset_counters<NT>(sm);
 
     for (;;) {
         if (threadIdx.x == 0) sm.item = atomicAdd(A.work_counter, 1);
@@ -64,9 +64,31 @@ __global__ void __launch_bounds__(NT, MINB) k_update(const __grid_constant__ Upd
         const int item = sm.item;
         __syncthreads();
         if (item >= nwork) break;
-        process_root<NT, ILP>(A.f, sm, W, A.worklist[item], A.all_visible != 0, c1, c2);
+        process_root<NT, ILP>(A.f, sm, W, A.worklist[item], A.all_visible != 0);
     }
-    flush_counters<NT>(sm, A.counters, c1, c2);
+    flush_counters<NT>(sm, A.counters);
+}
+
+// Deletions (one launch per deletion, after k_classify_delete): its own
+// kernel, so the insertion kernel's code and registers are untouched; any
+// launch shape fits the forest's worker scratch, since it only indexes worker
+// slots below its grid.
+template <int NT, int MINB, int ILP>
+__global__ void __launch_bounds__(NT, MINB) k_delete(const __grid_constant__ UpdateArgs A)
+{
+    __shared__ UpdSmem<NT> sm;
+    const Scratch W = A.scr.of(blockIdx.x, A.f.G.nv);
+    const int nwork = *A.nwork;
+    reset_counters<NT>(sm);
+    for (;;) {
+        if (threadIdx.x == 0) sm.item = atomicAdd(A.work_counter, 1);
+        __syncthreads();
+        const int item = sm.item;
+        __syncthreads();
+        if (item >= nwork) break;
+        process_deletion<NT, ILP>(A.f, sm, W, A.worklist[item], A.del_u, A.del_v);
+    }
+    flush_counters<NT>(sm, A.counters);
 }
 
 __global__ void k_classify(const int32_t* __restrict__ dist, int64_t nv, int nk, int nins,
@@ -136,6 +158,58 @@ constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 // batch hit L2 instead of HBM.
 constexpr int kDefaultVariant = 7;
 
+// Deletion of (u, v), already removed from the adjacency: warp per root.  A
+// root whose endpoints sit on the same level (or are both unreachable) is
+// unaffected; otherwise the deeper endpoint b either keeps a parent (a
+// neighbour one level up) -- sigma-only update, work list -- or has none and
+// its subtree moves down -- recompute list (the reference's split,
+// src/streamingbc.c:300-345).
+__global__ void k_classify_delete(const int32_t* __restrict__ dist, int64_t nv, int nk, DevGraph G, int u, int v,
+                                  const int* __restrict__ removed, int* __restrict__ adj, int* __restrict__ nadj,
+                                  int* __restrict__ mov, int* __restrict__ nmov, unsigned long long* counters)
+{
+    const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (r >= nk || *removed != 1) return;
+    const int32_t* D = dist + (size_t)r * nv;
+    const int du = D[u], dv = D[v];
+    if (du == dv) return;
+    const int b = du > dv ? u : v;
+    const int lb = du > dv ? du : dv;
+    const int64_t rb = G.row[b];
+    const int db = G.deg[b];
+    bool parent = false;
+    for (int base = 0; base < db && !parent; base += 32) {
+        const int s = base + lane;
+        parent = __any_sync(0xffffffffu, s < db && D[G.col[rb + s]] == lb - 1);
+    }
+    if (lane == 0) {
+        if (parent) {
+            adj[atomicAdd(nadj, 1)] = r;
+        } else {
+            mov[atomicAdd(nmov, 1)] = r;
+            atomicAdd(&counters[3], 1ull);
+        }
+    }
+}
+
+// bc[v] += sign * delta[r][v] (v != root) for every root r of the list.
+__global__ void k_bc_rows(const double* __restrict__ delta, const int64_t* __restrict__ roots,
+                          const int* __restrict__ list, const int* __restrict__ nlist, int64_t nv, double* bc,
+                          double sign)
+{
+    const int n = *nlist;
+    for (int i = blockIdx.y; i < n; i += gridDim.y) {
+        const int r = list[i];
+        const int64_t root = roots[r];
+        const double* Dl = delta + (size_t)r * nv;
+        for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < nv; x += (int64_t)gridDim.x * blockDim.x) {
+            const double d = Dl[x];
+            if (d != 0.0 && x != root) atomicAdd(&bc[x], sign * d);
+        }
+    }
+}
+
 int update_variant_count() { return kNumVariants; }
 int update_default_variant() { return kDefaultVariant; }
 int update_variant_threads(int v) { return kVariants[v].threads; }
@@ -167,6 +241,7 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     if (f->model && f->model->logging) A.f.cost_log = f->model->d_cost_log;
     A.scr = f->scratch();
     A.all_visible = all_visible ? 1 : 0;
+    A.del_u = A.del_v = 0;
     A.worklist = f->d_worklist;
     A.nwork = f->d_nwork;
     A.work_counter = f->d_counter;
@@ -178,6 +253,41 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     if ((e = cudaGetLastError())) return e;
     if ((e = launch_log_append(f, n))) return e;
     return launch_roster_compact(f, s);
+}
+
+cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)
+{
+    sbc_graph* g = f->g;
+    cudaStream_t s = g->stream;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(f->d_nwork, 0, 2 * sizeof(int), s)) || (e = cudaMemsetAsync(f->d_nmov, 0, 2 * sizeof(int), s)))
+        return e;
+    k_classify_delete<<<(int)((f->nk * 32 + 255) / 256), 256, 0, s>>>(f->d_dist, f->nv, (int)f->nk, g->dev(), u, v,
+                                                                      d_removed, f->d_worklist, f->d_nwork, f->d_mov,
+                                                                      f->d_nmov, f->d_counters);
+    if ((e = cudaGetLastError())) return e;
+    // roots that keep a parent of the deeper endpoint: incremental
+    UpdateArgs A;
+    A.f = forest_slot(f, 0);
+    A.scr = f->scratch();
+    A.all_visible = 1;
+    A.del_u = u;
+    A.del_v = v;
+    A.worklist = f->d_worklist;
+    A.nwork = f->d_nwork;
+    A.work_counter = f->d_counter;
+    A.counters = f->d_counters;
+    k_delete<512, 1, 4><<<(int)std::min<int64_t>(f->workers, f->nk), 512, 0, s>>>(A);
+    if ((e = cudaGetLastError())) return e;
+    // the others: old dependencies out of BC, recompute, new ones in
+    const dim3 grid((unsigned)std::min<int64_t>((f->nv + 255) / 256, 64), (unsigned)std::min<int64_t>(f->nk, 4096));
+    k_bc_rows<<<grid, 256, 0, s>>>(f->d_delta, f->d_roots, f->d_mov, f->d_nmov, f->nv, f->d_bc, -1.0);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = launch_static_list(f, f->d_mov, f->d_nmov))) return e;
+    k_bc_rows<<<grid, 256, 0, s>>>(f->d_delta, f->d_roots, f->d_mov, f->d_nmov, f->nv, f->d_bc, 1.0);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = launch_level_hist_list(f, f->d_mov, f->d_nmov))) return e;
+    return launch_roster_build_list(f, f->d_mov, f->d_nmov);
 }
 
 }  // namespace sbc

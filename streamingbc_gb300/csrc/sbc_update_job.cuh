@@ -18,6 +18,7 @@ struct UpdSmem {
     long long part[3 * (NT / 32) + 3];
     int item, qt, at, st;
     int nscan, nprobe;  // level-2 vertices whose parents are found by scan / by probe
+    unsigned long long c1, c2;  // case-1 / case-2 jobs of this CTA (written by thread 0)
 };
 
 // A level-2 vertex looks its parents up by binary search (one probe per root
@@ -25,9 +26,16 @@ struct UpdSmem {
 // many times the root's degree; a probe is costed as this many scanned slots.
 constexpr int kProbeRatio = 32;
 
+// One job: the insertion of edge (a, b) (a the shallower endpoint) on root r,
+// or with `del` the deletion of that edge when b keeps another parent (the
+// edge is already gone from the adjacency; |d| == 1, levels do not change).
+// A deletion is the insertion's sigma-only case with the paths through a
+// taken away (diffPath -sigma[a]) and, since b no longer reaches a through
+// the adjacency, b's old contribution to a taken out when b is committed
+// (removeEdgeWithoutMovementBrandes, src/streamingbc_internal.c:607-868).
 template <int NT, int ILP>
 __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r,
-                                        int a, int b, bool moving, int g)
+                                        int a, int b, bool moving, int g, bool del = false)
 {
     const int64_t nv = A.G.nv;
     int32_t* D = A.dist + (size_t)r * nv;
@@ -39,7 +47,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
 
     if (threadIdx.x == 0) {
         W.st[b] = 1;
-        W.dp[b] = S[a];
+        W.dp[b] = del ? -S[a] : S[a];
         W.qd[0] = b;
         W.lvl[0] = 0;
         W.lvl[1] = 1;
@@ -142,6 +150,12 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
         if (x != root) atomicAdd(&A.bc[x], nD - oD);
         S[x] = nS;
         Dl[x] = nD;
+        if (del && x == b) {
+            // a (one level up, not in the descent) loses b's old contribution
+            int old = atomicOr(&W.st[a], SBC_ASC);
+            if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = a;
+            atomicAdd(&W.acc[a], wd - wn);
+        }
     };
     auto prep = [&](int j, int x, int d) {
         double wn, wd;
@@ -440,7 +454,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
 // job, |d| == 1 (case 1) or |d| > 1 / one endpoint unreachable (case 2).
 template <int NT, int ILP>
 __device__ __forceinline__ void process_root(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r,
-                                             bool all_visible, unsigned long long& c1, unsigned long long& c2)
+                                             bool all_visible)
 {
     const int32_t* D = A.dist + (size_t)r * A.G.nv;
     for (int i = 0; i < A.nins; ++i) {
@@ -453,8 +467,8 @@ __device__ __forceinline__ void process_root(const ForestSlot& A, UpdSmem<NT>& s
         const int db = du > dv ? du : dv, da = du > dv ? dv : du;
         const bool moving = (db == SBC_INF) || (db - da > 1);
         if (threadIdx.x == 0) {
-            if (moving) c2++;
-            else c1++;
+            if (moving) sm.c2 += 1;
+            else sm.c1 += 1;
         }
         const unsigned long long walked0 = sm.lb.walked_v;  // read before run_job's first barrier
         run_job<NT, ILP>(A, sm, W, r, a, b, moving, all_visible ? INT_MAX : i);
@@ -463,16 +477,35 @@ __device__ __forceinline__ void process_root(const ForestSlot& A, UpdSmem<NT>& s
     }
 }
 
+// The deletion of (u, v) on root r, which keeps a parent of the deeper
+// endpoint (the classify step sends the other roots to a recompute).
+template <int NT, int ILP>
+__device__ __forceinline__ void process_deletion(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r,
+                                                 int u, int v)
+{
+    const int32_t* D = A.dist + (size_t)r * A.G.nv;
+    const int du = D[u], dv = D[v];
+    if (du == dv) return;
+    if (threadIdx.x == 0) sm.c1 += 1;
+    run_job<NT, ILP>(A, sm, W, r, du < dv ? u : v, du < dv ? v : u, false, INT_MAX, true);
+}
+
+// Zeroes the CTA's traversal and case counters (thread 0, before the first barrier).
+template <int NT>
+__device__ __forceinline__ void reset_counters(UpdSmem<NT>& sm)
+{
+    if (threadIdx.x == 0) sm.lb.walked_v = sm.lb.walked_e = sm.lb.scanned_e = sm.c1 = sm.c2 = 0;
+}
+
 // Adds the CTA's traversal and case counters into counters[0..4].
 template <int NT>
-__device__ __forceinline__ void flush_counters(UpdSmem<NT>& sm, unsigned long long* counters, unsigned long long c1,
-                                               unsigned long long c2)
+__device__ __forceinline__ void flush_counters(UpdSmem<NT>& sm, unsigned long long* counters)
 {
     if (threadIdx.x == 0) {
         atomicAdd(&counters[0], sm.lb.walked_v);
         atomicAdd(&counters[1], sm.lb.walked_e);
-        atomicAdd(&counters[2], c1);
-        atomicAdd(&counters[3], c2);
+        atomicAdd(&counters[2], sm.c1);
+        atomicAdd(&counters[3], sm.c2);
         atomicAdd(&counters[4], sm.lb.scanned_e);
     }
 }

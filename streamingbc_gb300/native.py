@@ -131,6 +131,9 @@ def load(path: str = LIB_PATH):
         "sbc_get_level_hist": (C.c_int, [_vp, C.c_int64, C.c_int64, _i32p]),
         "sbc_get_roster": (C.c_int, [_vp, C.c_int64, C.c_int, _i32p, C.POINTER(C.c_int)]),
         "sbc_insert_batch_async": (C.c_int, [_vp, C.c_int64, _i64p, _i64p]),
+        "sbc_delete_batch": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.POINTER(BatchStats)]),
+        "sbc_update_deleted": (C.c_int, [_vp, C.c_int64, C.c_int64, C.POINTER(BatchStats)]),
+        "sbc_graph_remove_directed": (C.c_int, [_vp, C.c_int64, C.c_int64, C.POINTER(C.c_int)]),
         "sbc_server_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.c_int64, C.c_int]),
         "sbc_server_destroy": (C.c_int, [_vp]),
         "sbc_server_set_max_inflight": (C.c_int, [_vp, C.c_int]),
@@ -198,6 +201,12 @@ class DeviceGraph:
         self.h = h
         self.nv = int(nv)
         self._forests = weakref.WeakSet()
+
+    def remove_directed(self, u: int, v: int) -> int:
+        """Remove u -> v: 1 removed, 0 absent, -1 invalid."""
+        r = C.c_int(0)
+        _check(self.lib.sbc_graph_remove_directed(self.h, int(u), int(v), C.byref(r)))
+        return r.value
 
     def degree(self, v: int) -> int:
         d = C.c_int64()
@@ -273,6 +282,22 @@ class DeviceForest:
         v = np.ascontiguousarray(pairs[:, 1])
         st = BatchStats()
         _check(self.lib.sbc_insert_batch(self.h, u.size, p64(u), p64(v), C.byref(st)))
+        return st.as_dict()
+
+    def delete(self, pairs) -> dict:
+        """Remove each edge (both directions) and update every root, one
+        deletion at a time; stats: inserted = removed, duplicates = absent."""
+        pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+        u = np.ascontiguousarray(pairs[:, 0])
+        v = np.ascontiguousarray(pairs[:, 1])
+        st = BatchStats()
+        _check(self.lib.sbc_delete_batch(self.h, u.size, p64(u), p64(v), C.byref(st)))
+        return st.as_dict()
+
+    def update_deleted(self, u: int, v: int) -> dict:
+        """The update for a deletion whose edge was already removed from the graph."""
+        st = BatchStats()
+        _check(self.lib.sbc_update_deleted(self.h, int(u), int(v), C.byref(st)))
         return st.as_dict()
 
     def insert_async(self, pairs):

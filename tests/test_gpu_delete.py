@@ -1,0 +1,146 @@
+"""Edge deletion on the GPU.  The state after a deletion is, by definition, a
+static recompute of the modified graph; the oracle does exactly that (the
+reference's own deletion path disagrees with it, see test_oracle.py)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from _util import assert_bc, assert_levels, assert_sigma
+from streamingbc_gb300 import graphs as G
+from streamingbc_gb300 import native
+
+pytestmark = pytest.mark.gpu
+
+
+def _edges(g):
+    src = np.repeat(np.arange(g.nv), np.diff(g.off))
+    sel = src < g.adj
+    return np.stack([src[sel], g.adj[sel]], axis=1)
+
+
+def _check(f, o):
+    assert_levels(f.level64(), o.level())
+    assert_sigma(f.sigma(), o.sigma(), o.level())
+    assert_bc(f.bc(), o.bc())
+
+
+def test_deletions_one_at_a_time_exact_er(sbc_lib, port_lib):
+    """ER 200/800, exact BC (K = 200): 40 deletions, state after each."""
+    g = G.er(200, 800, seed=5)
+    roots = G.pick_roots(g.nv, g.nv, seed=5)
+    rng = np.random.default_rng(5)
+    dels = _edges(g)[rng.choice(g.ne, 40, replace=False)]
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    moved = adjacent = 0
+    for u, v in dels:
+        assert o.delete(int(u), int(v))
+        st = f.delete([(u, v)])
+        assert st["inserted"] == 1
+        moved += st["case2"]
+        adjacent += st["case1"]
+        _check(f, o)
+    assert moved > 0 and adjacent > 0  # both the incremental and the recompute path ran
+    f.close()
+    dg.close()
+
+
+def test_rmat_deletions_between_insertion_batches(sbc_lib, port_lib):
+    """R-MAT scale 10 with degree-1 roots (rosters in use): insertion batches
+    and deletions (of original and of newly inserted edges) interleaved."""
+    g = G.rmat(10, 8, seed=9)
+    deg = np.diff(g.off)
+    rng = np.random.default_rng(9)
+    roots = np.unique(np.concatenate([rng.choice(np.nonzero(deg == 1)[0], 16, replace=False),
+                                      G.pick_roots(g.nv, 32, seed=9)]))
+    ins = G.rmat_insertions(g, 10, 96, seed=9)
+    orig = _edges(g)[rng.choice(g.ne, 48, replace=False)]
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    for k in range(3):
+        batch = ins[32 * k:32 * (k + 1)]
+        for u, v in batch:
+            o.insert(int(u), int(v))
+        f.insert(batch)
+        _check(f, o)
+        dels = np.concatenate([orig[16 * k:16 * (k + 1)], batch[:4]])
+        for u, v in dels:
+            o.delete(int(u), int(v))
+        f.delete(dels)
+        _check(f, o)
+    f.close()
+    dg.close()
+
+
+def test_absent_and_invalid_deletions(sbc_lib, port_lib):
+    g = G.er(100, 300, seed=2)
+    roots = G.pick_roots(g.nv, 20, seed=2)
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    before = (f.dist().copy(), f.sigma().copy(), f.bc().copy())
+    present = set(map(tuple, _edges(g).tolist()))
+    absent = next((u, v) for u in range(100) for v in range(u + 1, 100) if (u, v) not in present)
+    st = f.delete([absent, (3, 3), (-1, 5), (7, 10 ** 6)])
+    assert st["inserted"] == 0 and st["duplicates"] == 1 and st["invalid"] == 3
+    np.testing.assert_array_equal(f.dist(), before[0])
+    np.testing.assert_array_equal(f.sigma(), before[1])
+    np.testing.assert_array_equal(f.bc(), before[2])
+    f.close()
+    dg.close()
+
+
+def test_caller_removes_then_updates(sbc_lib, port_lib):
+    """The drop-in order: the caller removes both directions
+    (stinger_remove_edge x2), then asks for the update."""
+    g = G.er(150, 500, seed=3)
+    roots = G.pick_roots(g.nv, 40, seed=3)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    for u, v in _edges(g)[:20]:
+        assert dg.remove_directed(u, v) == 1 and dg.remove_directed(v, u) == 1
+        assert dg.remove_directed(u, v) == 0
+        f.update_deleted(u, v)
+        o.delete(int(u), int(v))
+        _check(f, o)
+    f.close()
+    dg.close()
+
+
+def test_rmat16_deletions_equal_static_recompute(sbc_lib):
+    """R-MAT 16, K = 256: 96 deletions then a fresh static init of the final
+    graph gives the same state (size-independent property)."""
+    g = G.rmat(16, 16, seed=3)
+    roots = G.pick_roots(g.nv, 256, seed=3)
+    rng = np.random.default_rng(3)
+    dels = _edges(g)[rng.choice(g.ne, 96, replace=False)]
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    st = f.delete(dels)
+    assert st["inserted"] == 96
+    keep = set(map(tuple, dels.tolist()))
+    e = [(a, b) for a, b in _edges(g).tolist() if (a, b) not in keep]
+    e = np.asarray(e, dtype=np.int64)
+    g2 = G.from_edges(g.nv, e[:, 0], e[:, 1])
+    dg2 = native.DeviceGraph(g2.nv, g2.off, g2.adj)
+    f2 = native.DeviceForest(dg2, roots)
+    f2.static_init()
+    np.testing.assert_array_equal(f.dist(), f2.dist())
+    reach = f2.dist() != np.iinfo(np.int32).max
+    np.testing.assert_array_equal(f.sigma()[reach], f2.sigma()[reach])
+    assert_bc(f.bc(), f2.bc())
+    for x in (f, f2):
+        x.close()
+    dg.close()
+    dg2.close()

@@ -83,6 +83,54 @@ def test_port_matches_compiled_reference_random(port_lib):
     o.close()
 
 
+def test_oracle_deletion_is_static_recompute(port_lib):
+    """PortOracle.delete = a fresh static init of the graph without the edge."""
+    g = G.er(80, 240, seed=4)
+    roots = G.pick_roots(g.nv, g.nv, 4)
+    src = np.repeat(np.arange(g.nv), np.diff(g.off))
+    edges = [(int(a), int(b)) for a, b in zip(src, g.adj) if a < b]
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    gone = edges[:10]
+    for u, v in gone:
+        assert o.delete(u, v)
+    assert not o.delete(*gone[0])  # already removed
+    rest = np.asarray([e for e in edges if e not in gone])
+    g2 = G.from_edges(g.nv, rest[:, 0], rest[:, 1])
+    o2 = port_lib.PortOracle(g2.nv, g2.off, g2.adj, roots)
+    o2.static()
+    assert_levels(o.level(), o2.level())
+    assert_sigma(o.sigma(), o2.sigma(), o2.level())
+    assert_bc(o.bc(), o2.bc())
+    o.close()
+    o2.close()
+
+
+def test_reference_deletion_disagrees_with_recompute(port_lib):
+    """The reference's deleteEdgeStreamingBC (src/streamingbc.c:258-416, with
+    moveDownTreeBrandes, src/streamingbc_internal.c:880-1401) does not end in
+    the state of the modified graph: on ER 200/800, deleting (48,122) leaves
+    vertex 84 of root 140 at level 4 with sigma 10, where a recomputation has
+    level 3, sigma 1.  Deletions are therefore checked against the
+    recomputation, not against the reference."""
+    if not port_lib.ref_available():
+        pytest.skip("reference harness not built here")
+    g = G.er(200, 800, seed=5)
+    roots = G.pick_roots(g.nv, 200, seed=3)
+    r = port_lib.RefOracle(g.nv, g.off, g.adj, roots, nthreads=1)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    r.static()
+    o.static()
+    r.delete(48, 122)
+    assert o.delete(48, 122)
+    lv, sg, _, _ = r.dump()
+    i = int(np.nonzero(roots == 140)[0][0])
+    assert (lv[i, 84], sg[i, 84]) == (4, 10)
+    assert (o.level()[i, 84], o.sigma()[i, 84]) == (3, 1)
+    r.close()
+    o.close()
+
+
 def _check_simple(g: G.Graph):
     src = np.repeat(np.arange(g.nv), np.diff(g.off))
     assert np.all(src != g.adj), "self loop"
