@@ -66,6 +66,7 @@ def parse():
                    help="cost model: insertions whose per-job costs are logged for training "
                         "(-1 = 16384 on rmat20, else 0 = static schedule)")
     p.add_argument("--train-epochs", type=int, default=4)
+    p.add_argument("--deletions", type=int, default=33, help="edge deletions timed after the insertion passes")
     p.add_argument("--compare-batches", type=int, default=8,
                    help="batches timed under both schedules after training")
     p.add_argument("--roots", type=int, default=0,
@@ -761,11 +762,32 @@ def run_ours(args):
                "d2h_bytes_per_step": 8 * g.nv + 4 * B + 4 + 32,
                "p50_step_ms": float(np.percentile(lat, 50)), "p99_step_ms": float(np.percentile(lat, 99))}
 
+    # ---------------- deletions (after everything else: they change the graph) ----------------
+    deletions = None
+    if args.deletions:
+        src = np.repeat(np.arange(g.nv), np.diff(g.off))
+        sel = src < g.adj
+        E = np.stack([src[sel], g.adj[sel]], axis=1)
+        pick = E[np.random.default_rng(17).choice(len(E), args.deletions, replace=False)]
+        f.delete(pick[:1])  # warm-up deletion
+        t1 = time.perf_counter()
+        dst = f.delete(pick[1:])
+        del_s = time.perf_counter() - t1
+        deletions = {"value": (len(pick) - 1) / del_s, "unit": "deletions/s", "deletions": len(pick) - 1,
+                     "removed": dst["inserted"], "incremental_root_pairs": dst["case1"],
+                     "recomputed_roots": dst["case2"],
+                     "note": "sbc_delete_batch, host arrays, synchronous: per deletion the edge is removed, roots "
+                             "that keep a parent of the deeper endpoint are updated incrementally, the others "
+                             "recomputed from scratch"}
+
     cpu = None
     if not args.no_cpu and rank == 0:
         threads = os.cpu_count() or 1
         nr = args.cpu_roots or min(len(roots), 2 * threads)
         cpu = cpu_sample(g, roots, ins_all, nr, args.cpu_insertions, threads)
+        if deletions:
+            # a deletion on the CPU port is a recompute of every root
+            deletions["cpu_port_recompute_s_per_deletion"] = cpu["static_sample_s"] * len(roots) / nr
 
     info = f.info()
     if rank == 0:
@@ -797,6 +819,7 @@ def run_ours(args):
             # model schedule classify becomes features + 3 ordering kernels
             "gpu_launches": (9 if model_info else 6) * args.steps,
             "cost_model": model_info,
+            "deletions": deletions,
             "plain_gpu": plain,
             "latency_ms": {"batch_p50": batch_ms, "wall_ms_timed": wall_ms,
                            "per_insertion_in_batch": batch_ms},

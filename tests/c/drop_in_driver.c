@@ -2,7 +2,8 @@
  * A reference-style caller of the streamingbc.h API, written exactly as the
  * reference's own driver uses it (src/sbcMain.c, src/sbcMain_utils.c:306-338,
  * :458-471): CSR -> CreateStingerFromCSR -> forest + auxiliary arrays -> static
- * init -> for each insertion: stinger_insert_edge x2, insertEdgeStreamingBC.
+ * init -> for each insertion: stinger_insert_edge x2, insertEdgeStreamingBC;
+ * then for each deletion: stinger_remove_edge x2, deleteEdgeStreamingBC.
  * Compiled with plain gcc against include/streamingbc.h and linked to
  * libsbc_gb300.so; nothing in it knows about CUDA.
  *
@@ -81,6 +82,24 @@ int main(int argc, char **argv)
         fprintf(out, "\n");
     }
     fprintf(out, "degree0 %lld\n", (long long)stinger_outdegree(G, 0));
+
+    /* optional tail: deletions, as the reference's callers make them
+     * (stinger_remove_edge x2, then deleteEdgeStreamingBC) */
+    long long ND = 0;
+    if (fscanf(in, "%lld", &ND) != 1) ND = 0;
+    for (long long i = 0; i < ND; i++) {
+        long long u, v;
+        if (fscanf(in, "%lld %lld", &u, &v) != 2) return 3;
+        if (stinger_remove_edge(G, 0, u, v) != 1 || stinger_remove_edge(G, 0, v, u) != 1) return 6;
+        deleteEdgeStreamingBC(forest, G, u, v, roots, NK, NV, NT, aux, BALANCE, COARSE);
+        if (sbc_last_error()[0]) {
+            fprintf(stderr, "delete: %s\n", sbc_last_error());
+            return 7;
+        }
+        fprintf(out, "dbc %lld", i);
+        for (long long x = 0; x < NV; x++) fprintf(out, " %.17g", forest->totalBC[x]);
+        fprintf(out, "\n");
+    }
     streamingBCDeleteAuxilary(aux, NT, NV);
     streamingBCDeleteForestApproximate(&forest, NK, roots);
     stinger_free(G);

@@ -35,9 +35,13 @@ def test_c_driver_compiles(driver):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["karate", "er200sparse", "rmat9"])
-def test_reference_style_c_caller_matches_reference(driver, tmp_path, case):
+def test_reference_style_c_caller_matches_reference(driver, tmp_path, case, port_lib):
     z = load_golden(case)
     nv = int(z["nv"])
+    # deletions after the insertions: three original edges
+    src = np.repeat(np.arange(nv), np.diff(z["off"]))
+    orig = [(int(a), int(b)) for a, b in zip(src, z["adj"]) if a < b]
+    dels = [orig[i] for i in (0, len(orig) // 2, len(orig) - 1)]
     inp = tmp_path / "in.txt"
     with open(inp, "w") as fh:
         fh.write(f"{nv} {z['adj'].size} {z['roots'].size} {len(z['ins'])}\n")
@@ -45,6 +49,9 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case):
         fh.write(" ".join(map(str, z["adj"].tolist())) + "\n")
         fh.write(" ".join(map(str, z["roots"].tolist())) + "\n")
         for u, v in z["ins"].tolist():
+            fh.write(f"{u} {v}\n")
+        fh.write(f"{len(dels)}\n")
+        for u, v in dels:
             fh.write(f"{u} {v}\n")
     outp = tmp_path / "out.txt"
     r = subprocess.run([str(driver), str(inp), str(outp)], capture_output=True, text=True, timeout=300)
@@ -61,6 +68,8 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case):
             sg[int(p[1])] = np.array(p[2:], dtype=np.int64)
         elif p[0] == "degree0":
             deg0 = int(p[1])
+        elif p[0] == "dbc":
+            bc[("del", int(p[1]))] = np.array(p[2:], dtype=np.float64)
     assert bc_err(bc[-1], z["bc0"]) <= BC_RTOL
     for i in range(len(z["ins"])):
         assert bc_err(bc[i], z["bc_trace"][i]) <= BC_RTOL, f"bc after insertion {i}"
@@ -69,3 +78,12 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case):
     assert_sigma(np.stack([sg[r] for r in range(k)]), z["sigma1"], z["level1"])
     added = sum(1 for u, v in z["ins"].tolist() if 0 in (u, v))
     assert deg0 == int(z["off"][1] - z["off"][0]) + added
+    # deletions: BC after each equals a recompute of the modified graph
+    o = port_lib.PortOracle(nv, z["off"], z["adj"], z["roots"])
+    o.static()
+    for u, v in z["ins"].tolist():
+        o.insert(int(u), int(v))
+    for i, (u, v) in enumerate(dels):
+        assert o.delete(u, v)
+        assert bc_err(bc[("del", i)], o.bc()) <= BC_RTOL, f"bc after deletion {i}"
+    o.close()
