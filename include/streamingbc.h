@@ -23,8 +23,12 @@
  *     (movement = roots with |d| > 1, adjacent = roots with |d| == 1,
  *     sameLevel = roots left unchanged); the reference returns zeros.  The
  *     counters of aux[0] receive the reference's traversal counters.
- *   - Edge deletion (deleteEdgeStreamingBC, deleteVertexStreamingBC) is not
- *     provided: they change nothing, return zeros and set sbc_last_error().
+ *   - deleteEdgeStreamingBC (after the caller's stinger_remove_edge x2, as in
+ *     the reference) ends in the state of the modified graph -- the same as a
+ *     static recompute -- which the reference's own deletion does not; its
+ *     counts are adjacent = roots updated incrementally, movement = roots
+ *     recomputed.  deleteVertexStreamingBC is not provided: it changes
+ *     nothing, returns zeros and sets sbc_last_error().
  *   - Failures do not abort: functions keep their reference signatures and
  *     report through sbc_last_error() (NULL / zero results on failure).
  */
