@@ -334,6 +334,9 @@ int sbc_update_deleted(sbc_forest *f, int64_t u, int64_t v, sbc_batch_stats *sta
 /* Directed removal with stinger_remove_edge's result: 1 removed, 0 absent,
  * -1 self loop / bad id.  Synchronous. */
 int sbc_graph_remove_directed(sbc_graph *g, int64_t from, int64_t to, int *result);
+/* Live neighbours of v: *n = its degree; the first min(cap, *n) are copied to
+ * out (cap 0 / out NULL to query the degree).  Synchronous. */
+int sbc_graph_neighbors(sbc_graph *g, int64_t v, int64_t *out, int64_t cap, int64_t *n);
 
 /* Wait for all work queued on the forest's graph stream. */
 int sbc_sync(sbc_forest *f);

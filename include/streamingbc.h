@@ -27,8 +27,9 @@
  *     the reference) ends in the state of the modified graph -- the same as a
  *     static recompute -- which the reference's own deletion does not; its
  *     counts are adjacent = roots updated incrementally, movement = roots
- *     recomputed.  deleteVertexStreamingBC is not provided: it changes
- *     nothing, returns zeros and sets sbc_last_error().
+ *     recomputed.  deleteVertexStreamingBC deletes the vertex's edges one at
+ *     a time the same way and reports the former neighbours in
+ *     adjacencyArray / *adjacencySize (the reference leaves the size at 0).
  *   - Failures do not abort: functions keep their reference signatures and
  *     report through sbc_last_error() (NULL / zero results on failure).
  */

@@ -1085,6 +1085,23 @@ int sbc_forest_autotune(sbc_forest* f, int64_t n, const int64_t* u, const int64_
 
 // ------------------------------------------------------------------ deletions
 
+int sbc_graph_neighbors(sbc_graph* g, int64_t v, int64_t* out, int64_t cap, int64_t* n)
+{
+    if (!g || !n || v < 0 || v >= g->nv || cap < 0 || (cap > 0 && !out))
+        return fail(SBC_ERR_ARG, "sbc_graph_neighbors: bad arguments");
+    if (use_device(g->device)) return SBC_ERR_CUDA;
+    int32_t d = 0;
+    CK(cudaMemcpyAsync(&d, g->d_deg + v, sizeof d, cudaMemcpyDeviceToHost, g->stream));
+    CK(cudaStreamSynchronize(g->stream));
+    *n = d;
+    if (cap == 0 || d == 0) return SBC_OK;
+    const int64_t k = std::min<int64_t>(cap, d);
+    std::vector<int32_t> buf((size_t)k);
+    CK(cudaMemcpy(buf.data(), g->d_col + g->h_row[v], sizeof(int32_t) * k, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < k; ++i) out[i] = buf[i];
+    return SBC_OK;
+}
+
 int sbc_graph_remove_directed(sbc_graph* g, int64_t from, int64_t to, int* result)
 {
     if (!g || !result) return fail(SBC_ERR_ARG, "sbc_graph_remove_directed: bad arguments");
@@ -2120,17 +2137,38 @@ StreamingExtraInfo insertVertexStreamingBC(bcForest* forest, struct stinger* sSt
     return total;
 }
 
+// src/streamingbc.c:229-256: remove every edge of src, one at a time, each
+// followed by deleteEdgeStreamingBC.  adjacencyArray receives the former
+// neighbours and *adjacencySize their number (the reference intends this but
+// never advances its index, so it reports 0).
 StreamingExtraInfo deleteVertexStreamingBC(bcForest* forest, struct stinger* sStinger, int64_t src,
                                            int64_t* adjacencyArray, int64_t* adjacencySize,
                                            int64_t* rootArrayForApproximation, int64_t NK, int64_t NV, int64_t NT,
                                            extraArraysPerThread** eAPT)
 {
-    (void)forest; (void)sStinger; (void)src; (void)adjacencyArray; (void)rootArrayForApproximation;
-    (void)NK; (void)NV; (void)NT; (void)eAPT;
+    StreamingExtraInfo total = {0, 0, 0, 0};
     if (adjacencySize) *adjacencySize = 0;
-    fail(SBC_ERR_UNSUPPORTED, "deleteVertexStreamingBC: edge deletion is not provided");
-    StreamingExtraInfo sei = {0, 0, 0, 0};
-    return sei;
+    if (!sStinger || !sStinger->g) {
+        fail(SBC_ERR_STATE, "deleteVertexStreamingBC: no graph");
+        return total;
+    }
+    int64_t n = 0;
+    if (sbc_graph_neighbors(sStinger->g, src, nullptr, 0, &n)) return total;
+    std::vector<int64_t> nbr((size_t)n);
+    if (n && sbc_graph_neighbors(sStinger->g, src, nbr.data(), n, &n)) return total;
+    for (int64_t d = 0; d < n; ++d) {
+        const int64_t dest = nbr[d];
+        if (adjacencyArray) adjacencyArray[d] = dest;
+        stinger_remove_edge(sStinger, 0, src, dest);
+        stinger_remove_edge(sStinger, 0, dest, src);
+        StreamingExtraInfo one = deleteEdgeStreamingBC(forest, sStinger, src, dest, rootArrayForApproximation, NK, NV,
+                                                       NT, eAPT, BALANCE, FINE);
+        total.adjacent += one.adjacent;
+        total.movement += one.movement;
+        total.sameLevel += one.sameLevel;
+    }
+    if (adjacencySize) *adjacencySize = n;
+    return total;
 }
 
 int streamingBCSyncForest(bcForest* forest)

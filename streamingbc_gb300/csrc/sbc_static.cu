@@ -44,6 +44,7 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
     __shared__ int s_item, s_tail;
     __shared__ int64_t s_sig[NT];
     __shared__ double s_acc[NT];
+    __shared__ int s_hit[NT];
     const int64_t nv = A.nv;
     Scratch W = A.scr.of(blockIdx.x, nv);
     if (threadIdx.x == 0) sm.walked_v = sm.walked_e = sm.scanned_e = 0;
@@ -108,14 +109,24 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         __syncthreads();
         const int nlev = L;  // levels 0 .. nlev-1 are non-empty
 
-        // Backward: deepest level first; w[x] lives in the worker's acc array.
+        // Backward: deepest level first; w[x] = (delta[x]+1)/sigma[x] lives in
+        // the worker's acc array.  Each vertex sums its children's w with the
+        // summing walker (per-thread running sums, warp-combined), not one
+        // shared fp64 atomic per child edge: a hub's children would all hit
+        // one address, and GB300's fp64 rate is a small fraction of its fp32.
         for (int l = nlev - 1; l >= 0; --l) {
             const int b0 = W.lvl[l], b1 = W.lvl[l + 1];
-            lb_walk<NT>(
-                A.G, INT_MAX, D, D8, W.qd + b0, b1 - b0, nullptr, 0, sm,
-                [&](int j, int x, int d) { s_acc[j] = 0.0; },
-                [&](int j, int x, int k, int dk) {
-                    if (dk == l + 1) atomicAdd(&s_acc[j], W.acc[k]);
+            lb_walk_sum<NT, true>(
+                A.G, INT_MAX, D, D8, W.qd + b0, b1 - b0, sm, s_acc, s_hit,
+                [&](int j, int x, int d) {
+                    s_hit[j] = 0;
+                    atomicAdd(&sm.walked_v, 1ull);  // reference counters: walked vertex and its degree
+                    atomicAdd(&sm.walked_e, (unsigned long long)d);
+                },
+                [&](int j, int x, int k, int dk, double& v) -> bool {
+                    if (dk != l + 1) return false;
+                    v = W.acc[k];
+                    return true;
                 },
                 [&](int j, int x) {
                     double sx = (double)Sg[x];

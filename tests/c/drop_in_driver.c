@@ -3,7 +3,8 @@
  * reference's own driver uses it (src/sbcMain.c, src/sbcMain_utils.c:306-338,
  * :458-471): CSR -> CreateStingerFromCSR -> forest + auxiliary arrays -> static
  * init -> for each insertion: stinger_insert_edge x2, insertEdgeStreamingBC;
- * then for each deletion: stinger_remove_edge x2, deleteEdgeStreamingBC.
+ * then for each deletion: stinger_remove_edge x2, deleteEdgeStreamingBC;
+ * then optionally deleteVertexStreamingBC of one vertex.
  * Compiled with plain gcc against include/streamingbc.h and linked to
  * libsbc_gb300.so; nothing in it knows about CUDA.
  *
@@ -99,6 +100,24 @@ int main(int argc, char **argv)
         fprintf(out, "dbc %lld", i);
         for (long long x = 0; x < NV; x++) fprintf(out, " %.17g", forest->totalBC[x]);
         fprintf(out, "\n");
+    }
+
+    /* optional: delete a whole vertex (deleteVertexStreamingBC) */
+    long long VD = -1;
+    if (fscanf(in, "%lld", &VD) != 1) VD = -1;
+    if (VD >= 0) {
+        int64_t *adj = (int64_t *)malloc(sizeof(int64_t) * (size_t)NV);
+        int64_t size = -1;
+        deleteVertexStreamingBC(forest, G, VD, adj, &size, roots, NK, NV, NT, aux);
+        if (sbc_last_error()[0]) {
+            fprintf(stderr, "delete vertex: %s\n", sbc_last_error());
+            return 8;
+        }
+        fprintf(out, "vdeg %lld %lld\n", (long long)size, (long long)stinger_outdegree(G, VD));
+        fprintf(out, "vbc 0");
+        for (long long x = 0; x < NV; x++) fprintf(out, " %.17g", forest->totalBC[x]);
+        fprintf(out, "\n");
+        free(adj);
     }
     streamingBCDeleteAuxilary(aux, NT, NV);
     streamingBCDeleteForestApproximate(&forest, NK, roots);

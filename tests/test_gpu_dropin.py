@@ -53,11 +53,12 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case, port
         fh.write(f"{len(dels)}\n")
         for u, v in dels:
             fh.write(f"{u} {v}\n")
+        fh.write("1\n")  # then delete vertex 1 with all its edges
     outp = tmp_path / "out.txt"
     r = subprocess.run([str(driver), str(inp), str(outp)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     bc, lv, sg = {}, {}, {}
-    deg0 = None
+    deg0 = vdeg = None
     for line in open(outp):
         p = line.split()
         if p[0] == "bc":
@@ -70,6 +71,10 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case, port
             deg0 = int(p[1])
         elif p[0] == "dbc":
             bc[("del", int(p[1]))] = np.array(p[2:], dtype=np.float64)
+        elif p[0] == "vbc":
+            bc["vertex"] = np.array(p[2:], dtype=np.float64)
+        elif p[0] == "vdeg":
+            vdeg = (int(p[1]), int(p[2]))
     assert bc_err(bc[-1], z["bc0"]) <= BC_RTOL
     for i in range(len(z["ins"])):
         assert bc_err(bc[i], z["bc_trace"][i]) <= BC_RTOL, f"bc after insertion {i}"
@@ -86,4 +91,12 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case, port
     for i, (u, v) in enumerate(dels):
         assert o.delete(u, v)
         assert bc_err(bc[("del", i)], o.bc()) <= BC_RTOL, f"bc after deletion {i}"
+    # vertex 1: all its edges, then BC of the graph without them
+    nb = [int(y) for y in z["adj"][z["off"][1]:z["off"][2]]]
+    nb += [v if u == 1 else u for u, v in z["ins"].tolist() if 1 in (u, v)]
+    nb = [y for y in dict.fromkeys(nb) if (min(1, y), max(1, y)) not in set(dels)]
+    for y in nb:
+        o.delete(1, y)
+    assert vdeg == (len(nb), 0)
+    assert bc_err(bc["vertex"], o.bc()) <= BC_RTOL
     o.close()
