@@ -375,6 +375,12 @@ cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed);
 // Static recompute of the roots listed (device list and count) or, with a
 // null list, of all roots.
 cudaError_t launch_static_list(sbc_forest* f, const int* d_list, const int* d_nlist);
+// Whole-GPU recompute of root row r (level-synchronous, synchronous); used by
+// deletions on graphs of at least kWideRecomputeMinVertices vertices for up to
+// kWideRecompute roots, the static kernel otherwise.
+cudaError_t recompute_root_wide(sbc_forest* f, int r);
+constexpr int kWideRecompute = 64;
+constexpr int64_t kWideRecomputeMinVertices = 32768;
 cudaError_t launch_level_hist_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 cudaError_t launch_roster_build_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 // Cost model and schedule (sbc_model.cu).

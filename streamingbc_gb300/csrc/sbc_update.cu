@@ -33,6 +33,7 @@
 // Results are exact for dist/sigma (integer atomics); BC/delta differ from the
 // reference only by floating-point summation order.
 #include <climits>
+#include <vector>
 #include "sbc_host.h"
 #include "sbc_internal.cuh"
 #include "sbc_update_job.cuh"
@@ -279,11 +280,27 @@ cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)
     A.counters = f->d_counters;
     k_delete<512, 1, 4><<<(int)std::min<int64_t>(f->workers, f->nk), 512, 0, s>>>(A);
     if ((e = cudaGetLastError())) return e;
-    // the others: old dependencies out of BC, recompute, new ones in
+    // the others: old dependencies out of BC, recompute, new ones in.  On a
+    // large graph a few roots are recomputed one at a time by the whole GPU
+    // (one CTA would walk the whole graph alone); otherwise the static kernel
+    // recomputes them at once, a CTA per root.
+    int nmov = 0;
+    if ((e = cudaMemcpyAsync(&nmov, f->d_nmov, sizeof(int), cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+        return e;
+    if (nmov == 0) return cudaSuccess;
     const dim3 grid((unsigned)std::min<int64_t>((f->nv + 255) / 256, 64), (unsigned)std::min<int64_t>(f->nk, 4096));
     k_bc_rows<<<grid, 256, 0, s>>>(f->d_delta, f->d_roots, f->d_mov, f->d_nmov, f->nv, f->d_bc, -1.0);
     if ((e = cudaGetLastError())) return e;
-    if ((e = launch_static_list(f, f->d_mov, f->d_nmov))) return e;
+    if (nmov <= kWideRecompute && f->nv >= kWideRecomputeMinVertices) {
+        std::vector<int> rows(nmov);
+        if ((e = cudaMemcpyAsync(rows.data(), f->d_mov, sizeof(int) * nmov, cudaMemcpyDeviceToHost, s)) ||
+            (e = cudaStreamSynchronize(s)))
+            return e;
+        for (int r : rows)
+            if ((e = recompute_root_wide(f, r))) return e;
+    } else if ((e = launch_static_list(f, f->d_mov, f->d_nmov))) {
+        return e;
+    }
     k_bc_rows<<<grid, 256, 0, s>>>(f->d_delta, f->d_roots, f->d_mov, f->d_nmov, f->nv, f->d_bc, 1.0);
     if ((e = cudaGetLastError())) return e;
     if ((e = launch_level_hist_list(f, f->d_mov, f->d_nmov))) return e;

@@ -144,3 +144,68 @@ def test_rmat16_deletions_equal_static_recompute(sbc_lib):
         x.close()
     dg.close()
     dg2.close()
+
+
+def test_bridge_deletions_recompute_many_roots(sbc_lib, port_lib):
+    """A random tree plus a few chords: deleting a bridge leaves the deeper
+    endpoint without a parent for most roots, so one deletion recomputes many
+    roots at once (the static kernel path on small graphs)."""
+    rng = np.random.default_rng(12)
+    n = 300
+    par = np.array([rng.integers(0, i) for i in range(1, n)])
+    tree = np.stack([par, np.arange(1, n)], axis=1)
+    chords = rng.integers(0, n, size=(40, 2))
+    chords = chords[chords[:, 0] != chords[:, 1]]
+    e = np.concatenate([tree, chords])
+    g = G.from_edges(n, np.minimum(e[:, 0], e[:, 1]), np.maximum(e[:, 0], e[:, 1]))
+    roots = G.pick_roots(n, 120, seed=12)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    most = 0
+    for u, v in list(tree[rng.choice(len(tree), 6, replace=False)]) + list(_edges(g)[:6]):
+        if not o.delete(int(u), int(v)):
+            continue
+        st = f.delete([(u, v)])
+        most = max(most, st["case2"])
+        _check(f, o)
+    assert most > 16
+    f.close()
+    dg.close()
+
+
+def test_wide_recompute_on_large_graph(sbc_lib):
+    """On a graph of >= 32768 vertices a deletion recomputes its few affected
+    roots with the whole GPU; the result equals a static init of the graph
+    without the edges."""
+    g = G.chung_lu(40000, 120000, 2.5, 1.0, 200.0, seed=21)
+    roots = G.pick_roots(g.nv, 48, seed=21)
+    rng = np.random.default_rng(21)
+    deg = np.diff(g.off)
+    src = np.repeat(np.arange(g.nv), deg)
+    # edges to degree-1 vertices: deleting one disconnects it for every root
+    leaf_edges = np.stack([src, g.adj], axis=1)[(deg[g.adj] == 1) & (src < g.adj) | (deg[src] == 1) & (src < g.adj)]
+    dels = np.concatenate([leaf_edges[rng.choice(len(leaf_edges), 4, replace=False)],
+                           _edges(g)[rng.choice(g.ne, 12, replace=False)]])
+    dels = np.unique(dels, axis=0)
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    st = f.delete(dels)
+    assert st["case2"] > 0 and st["inserted"] == len(dels)
+    keep = set(map(tuple, dels.tolist()))
+    e = np.asarray([(a, b) for a, b in _edges(g).tolist() if (a, b) not in keep], dtype=np.int64)
+    g2 = G.from_edges(g.nv, e[:, 0], e[:, 1])
+    dg2 = native.DeviceGraph(g2.nv, g2.off, g2.adj)
+    f2 = native.DeviceForest(dg2, roots)
+    f2.static_init()
+    np.testing.assert_array_equal(f.dist(), f2.dist())
+    reach = f2.dist() != np.iinfo(np.int32).max
+    np.testing.assert_array_equal(f.sigma()[reach], f2.sigma()[reach])
+    assert_bc(f.bc(), f2.bc())
+    for x in (f, f2):
+        x.close()
+    dg.close()
+    dg2.close()
