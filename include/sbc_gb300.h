@@ -31,7 +31,7 @@ extern "C" {
 #define SBC_ERR_CUDA (-2)        /* CUDA runtime error (message in sbc_last_error) */
 #define SBC_ERR_NOMEM (-3)       /* device or host allocation failed */
 #define SBC_ERR_STATE (-4)       /* call out of order (e.g. insert before static init) */
-#define SBC_ERR_UNSUPPORTED (-5) /* operation not provided (vertex deletion) */
+#define SBC_ERR_UNSUPPORTED (-5) /* operation not provided (reserved; no entry point returns it) */
 #define SBC_ERR_NOGPU (-6)       /* no CUDA device */
 
 typedef struct sbc_graph sbc_graph;

@@ -11,7 +11,8 @@
  *   - each graph owns its storage (the reference's edge-block pool is process
  *     global and stinger_free releases it for every instance,
  *     src/stinger/stinger.c:557-568);
- *   - edge removal returns -1 (edge deletion is not provided).
+ *   - edge removal (src/stinger/stinger.c:1055-1090) compacts the slot out of
+ *     the vertex's sorted segment instead of marking it deleted.
  */
 #ifndef SBC_STINGER_SHIM_H_
 #define SBC_STINGER_SHIM_H_
@@ -44,7 +45,9 @@ int stinger_insert_edge(struct stinger *G, int64_t type, int64_t from, int64_t t
 int stinger_insert_edge_pair(struct stinger *G, int64_t type, int64_t from, int64_t to, int64_t weight,
                              int64_t timestamp);
 
-/* Edge removal is not provided: returns -1. */
+/* src/stinger/stinger.c:1055-1090 -- directed removal: 1 removed, -1 absent,
+ * self loop or invalid id (the reference's code returns -1 for an absent edge,
+ * although its comment says 0).  Synchronous (reads the result back). */
 int stinger_remove_edge(struct stinger *G, int64_t type, int64_t from, int64_t to);
 
 int64_t stinger_outdegree(const struct stinger *G, int64_t v);

@@ -1908,7 +1908,7 @@ int stinger_remove_edge(struct stinger* G, int64_t type, int64_t from, int64_t t
     if (!G || !G->g) return -1;
     int res = -1;
     if (sbc_graph_remove_directed(G->g, from, to, &res)) return -1;
-    return res;
+    return res == 1 ? 1 : -1;  // an absent edge falls through to -1 (src/stinger/stinger.c:1089)
 }
 
 int64_t stinger_outdegree(const struct stinger* G, int64_t v)

@@ -207,12 +207,49 @@ struct LbSmem {
 // HBM reads outstanding instead of one.
 constexpr int kEdgeIlp = 4;
 
+// Adjacency slots of one round of a walker chunk.  A chunk's `total` edges are
+// dealt out in rounds of NT * per, per = ceil(total / NT) capped at ILP: in
+// each round thread t takes the `per` consecutive edges from e0 = round start +
+// t * per.  Consecutive edges mostly share a source vertex, so a thread finds
+// its vertex with one binary search over the chunk's offsets per round and
+// then steps (a hub's adjacency costs no search per edge), while a chunk of at
+// most NT edges still gives every thread one edge and no thread a serial chain
+// of several.  Sets kk[u] (neighbour, -1 past the end) and jj[u] (chunk vertex)
+// for u < per; j is the thread's current chunk vertex, which only moves forward.
+template <int NT, int ILP>
+__device__ __forceinline__ void walk_fetch(const DevGraph& G, const LbSmem<NT>& sm, int cnt, int total, int e0,
+                                           int per, int& j, int (&kk)[ILP], int (&jj)[ILP])
+{
+#pragma unroll
+    for (int u = 0; u < ILP; ++u) {
+        const int e = e0 + u;
+        kk[u] = -1;
+        jj[u] = j;
+        if (u < per && e < total) {
+            if (sm.off[j + 1] <= e) {
+                int lo = j + 1, hi = cnt - 1;
+                // within a round the next edge is usually on the next vertex
+                // (off[j+1] <= e < total = off[cnt] keeps j + 2 <= cnt)
+                if (u > 0 && sm.off[j + 2] > e) hi = lo;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sm.off[mid] <= e) lo = mid;
+                    else hi = mid - 1;
+                }
+                j = lo;
+            }
+            jj[u] = j;
+            kk[u] = G.col[sm.row[j] + (e - sm.off[j])];
+        }
+    }
+}
+
 // Edge-balanced walk over the neighbours of a vertex list given as up to two
 // ranges (l1[0..n1) then l2[0..n2)).  Vertices are taken NT at a time; each
 // thread runs prep(j, x, visible_degree) for its vertex, an exclusive scan of
 // the visible degrees spreads the chunk's edges evenly over the block, and
-// edge(j, x, k, dist[k]) runs once per visible neighbour k (consecutive threads
-// read consecutive adjacency slots; the distance is gathered by the walker from
+// edge(j, x, k, dist[k]) runs once per visible neighbour k (slots dealt out by
+// walk_fetch, a warp reading one contiguous run; the distance is gathered from
 // the root's one-byte row D8, falling back to the int32 row D only for levels
 // >= 254).  post(j, x) runs after the chunk's edges.  Ends with a barrier.
 // REF: the walked vertices and their degrees count as traversed in the
@@ -249,27 +286,10 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t*
         }
         __syncthreads();
         int j = 0;  // chunk vertex of this thread's current edge; edges only move forward
-        for (int e0 = t; e0 < total; e0 += NT * ILP) {
+        const int per = min(ILP, (total + NT - 1) / NT);
+        for (int e0 = t * per; e0 < total; e0 += NT * per) {
             int kk[ILP], jj[ILP], dk[ILP];
-#pragma unroll
-            for (int u = 0; u < ILP; ++u) {
-                const int e = e0 + u * NT;
-                kk[u] = -1;
-                jj[u] = j;
-                if (e < total) {
-                    if (sm.off[j + 1] <= e) {
-                        int lo = j + 1, hi = cnt - 1;
-                        while (lo < hi) {
-                            int mid = (lo + hi + 1) >> 1;
-                            if (sm.off[mid] <= e) lo = mid;
-                            else hi = mid - 1;
-                        }
-                        j = lo;
-                    }
-                    jj[u] = j;
-                    kk[u] = G.col[sm.row[j] + (e - sm.off[j])];
-                }
-            }
+            walk_fetch<NT, ILP>(G, sm, cnt, total, e0, per, j, kk, jj);
 #pragma unroll
             for (int u = 0; u < ILP; ++u) dk[u] = kk[u] >= 0 ? (int)D8[kk[u]] : 0;
 #pragma unroll
@@ -332,27 +352,10 @@ __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const int3
         int j = 0;
         int cj = -1;       // source vertex of the running sum
         double cs = 0.0;   // running sum
-        for (int e0 = t; e0 < total; e0 += NT * ILP) {
+        const int per = min(ILP, (total + NT - 1) / NT);
+        for (int e0 = t * per; e0 < total; e0 += NT * per) {
             int kk[ILP], jj[ILP], dk[ILP];
-#pragma unroll
-            for (int u = 0; u < ILP; ++u) {
-                const int e = e0 + u * NT;
-                kk[u] = -1;
-                jj[u] = j;
-                if (e < total) {
-                    if (sm.off[j + 1] <= e) {
-                        int lo = j + 1, hi = cnt - 1;
-                        while (lo < hi) {
-                            int mid = (lo + hi + 1) >> 1;
-                            if (sm.off[mid] <= e) lo = mid;
-                            else hi = mid - 1;
-                        }
-                        j = lo;
-                    }
-                    jj[u] = j;
-                    kk[u] = G.col[sm.row[j] + (e - sm.off[j])];
-                }
-            }
+            walk_fetch<NT, ILP>(G, sm, cnt, total, e0, per, j, kk, jj);
 #pragma unroll
             for (int u = 0; u < ILP; ++u) dk[u] = (GATHER && kk[u] >= 0) ? (int)D8[kk[u]] : 0;
             if (GATHER) {
