@@ -39,7 +39,7 @@ __device__ __forceinline__ void append_warp(int64_t nv, const int64_t* __restric
         }
         if (code == 1 && !(deg[u] < cap[u] && (directed || deg[v] < cap[v]))) {
             code = -2;
-            if (lane == 0) atomicExch(err, 1);
+            if (lane == 0) atomicOr(err, 1);
         }
         if (lane == 0) {
             if (code == 1) {

@@ -316,110 +316,132 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 sm.lb.walked_e += (unsigned)vis_deg(A.G, x, A.G.row[x], g);
             }
             __syncthreads();
-        } else if (pull_ok) {
-            // Commit every vertex x of the level and keep its push weights in
-            // its acc/dp slots; count it as traversed (reference counters).
-            //   L == 1  the only parent is the root (sigma 1): each x's
-            //           contribution is summed straight into the root, no scan.
-            //   L == 2  parents are N(x) ∩ N(root).  Per vertex, either scan
-            //           N(x) for distance-1 neighbours (push), or, when N(x) is
-            //           much longer than N(root), look each root neighbour up
-            //           in x's sorted adjacency (probe); or, for the whole
-            //           level, let the root's neighbours pull (bitmap test).
-            //           The cheapest plan by scanned slots is taken.
-            const int na_ = ua_hi - ua_lo;
-            const int64_t rrow = A.G.row[root];
-            const int rdeg = vis_deg(A.G, root, rrow, g);
-            const bool rootDown = (W.st[root] & SBC_STEP_MASK) != 0;
-            long long push_cost = 0, mixed_cost = 0;
-            double root_sum = 0.0;
-            const int qbase = sm.st;  // free tail of the same-level queue holds the two lists
-            for (int i = threadIdx.x; i < dn + na_; i += NT) {
-                const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
-                double wn, wd;
-                commit(x, wn, wd);
-                W.acc[x] = wn;
-                W.dp[x] = (int64_t)__double_as_longlong(wd);
-                const int dx = vis_deg(A.G, x, A.G.row[x], g);
-                push_cost += dx;
-                if (L == 1) {
-                    root_sum += (rootDown || (root == a && x == b)) ? wn : wd;
-                } else if (L == 2) {
-                    atomicOr(&W.bits[x >> 5], 1u << (x & 31));
-                    if ((long long)dx > (long long)kProbeRatio * rdeg) {
-                        W.qs[nv - 1 - atomicAdd(&sm.nprobe, 1)] = x;
-                        mixed_cost += (long long)kProbeRatio * rdeg;
-                    } else {
-                        W.qs[qbase + atomicAdd(&sm.nscan, 1)] = x;
-                        mixed_cost += dx;
-                    }
-                }
-            }
-            block_sum3<NT>(push_cost, mixed_cost, root_sum, sm.part);
-            if (threadIdx.x == 0) {
-                sm.lb.walked_v += (unsigned)(dn + na_);
-                sm.lb.walked_e += (unsigned long long)push_cost;
-            }
-            if (L == 1) {
-                if (threadIdx.x == 0 && dn + na_ > 0) {
-                    W.acc[root] += root_sum;
-                    if (!rootDown) {
-                        int old = atomicOr(&W.st[root], SBC_ASC);
-                        if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = root;
-                    }
-                }
-                __syncthreads();
-            } else if (L == 2 && dn + na_ > 0) {
-                if (pull2_cost < 0) {
-                    long long c = 0;
-                    for (int i = threadIdx.x; i < rdeg; i += NT) {
-                        const int y = A.G.col[rrow + i];
-                        c += vis_deg(A.G, y, A.G.row[y], g);
-                    }
-                    pull2_cost = block_sum<NT>(c, sm.part);
-                }
-                if (pull2_cost < mixed_cost) {
-                    pull_walk(A.G.col + rrow, rdeg);
-                } else {
-                    const int nscan = sm.nscan, nprobe = sm.nprobe;
-                    lb_walk<NT, false, ILP>(A.G, g, D, D8, W.qs + qbase, nscan, nullptr, 0, sm.lb, prep_loaded,
-                                       [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
-                    probe_parents(W.qs + nv - nprobe, nprobe, A.G.col + rrow, rdeg, false);
-                }
-                for (int i = threadIdx.x; i < dn + na_; i += NT) {
-                    const int x = i < dn ? dlist[i] : W.qa[ua_lo + i - dn];
-                    W.bits[x >> 5] = 0u;  // words hold only this level's marks
-                }
-                __syncthreads();
-            }
-        } else if (!moving) {
-            lb_walk<NT, true, ILP>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep_div,
-                        [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
-            probe_diverted();
         } else {
-            const int same_lo = sm.st;
-            lb_walk<NT, true, ILP>(
-                A.G, g, D, D8, dlist, dn, nullptr, 0, sm.lb, prep,
-                [&](int j, int x, int k, int dk) {
-                    if (parent_edge(j, x, k, dk)) return;
-                    if (!(sm.fl[j] & 1) || dk != L) return;
-                    // k kept its level and lost the moved vertex x as a child
-                    const int sk = W.st[k];
-                    if (sk & SBC_STEP_MASK) return;
-                    if (!(sk & SBC_ASC)) {
-                        int old = atomicOr(&W.st[k], SBC_ASC);
-                        if (!(old & SBC_ASC)) {
-                            int p = atomicAdd(&sm.st, 1);
-                            W.qs[p] = k;
+            // Vertices whose parents the level-1/2 forms below find: the whole
+            // level where none of it moved; in a re-levelling job at levels 1-2,
+            // the second walk's vertices (ascent-only and same-level ones,
+            // none of which moved) once the moved ones have pushed.
+            const int32_t* nl1 = dlist;
+            const int32_t* nl2 = W.qa + ua_lo;
+            int nn1 = dn, nn2 = ua_hi - ua_lo;
+            bool near = pull_ok;
+            if (!pull_ok && !moving) {
+                lb_walk<NT, true, ILP>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep_div,
+                                       [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+                probe_diverted();
+            } else if (!pull_ok) {
+                const int same_lo = sm.st;
+                lb_walk<NT, true, ILP>(
+                    A.G, g, D, D8, dlist, dn, nullptr, 0, sm.lb, prep,
+                    [&](int j, int x, int k, int dk) {
+                        if (parent_edge(j, x, k, dk)) return;
+                        if (!(sm.fl[j] & 1) || dk != L) return;
+                        // k kept its level and lost the moved vertex x as a child
+                        const int sk = W.st[k];
+                        if (sk & SBC_STEP_MASK) return;
+                        if (!(sk & SBC_ASC)) {
+                            int old = atomicOr(&W.st[k], SBC_ASC);
+                            if (!(old & SBC_ASC)) {
+                                int p = atomicAdd(&sm.st, 1);
+                                W.qs[p] = k;
+                            }
+                        }
+                        atomicAdd(&W.acc[k], sm.wd[j] - sm.wn[j]);
+                    },
+                    NoPost());
+                const int same_hi = sm.st;
+                const int n2w = ua_hi - ua_lo + same_hi - same_lo;
+                // level 2 keeps its scan list after the same-level entries of
+                // the queue and its probe list at the queue's end
+                if (L == 1 || (L == 2 && (long long)same_hi + 2ll * n2w <= nv)) {
+                    near = true;
+                    nl1 = W.qa + ua_lo;
+                    nn1 = ua_hi - ua_lo;
+                    nl2 = W.qs + same_lo;
+                    nn2 = same_hi - same_lo;
+                } else {
+                    lb_walk<NT, true, ILP>(A.G, g, D, D8, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo,
+                                           same_hi - same_lo, sm.lb, prep_div,
+                                           [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+                    probe_diverted();
+                }
+            }
+            if (near) {
+                // Commit every vertex x of the level and keep its push weights in
+                // its acc/dp slots; count it as traversed (reference counters).
+                //   L == 1  the only parent is the root (sigma 1): each x's
+                //           contribution is summed straight into the root, no scan.
+                //   L == 2  parents are N(x) ∩ N(root).  Per vertex, either scan
+                //           N(x) for distance-1 neighbours (push), or, when N(x) is
+                //           much longer than N(root), look each root neighbour up
+                //           in x's sorted adjacency (probe); or, for the whole
+                //           level, let the root's neighbours pull (bitmap test).
+                //           The cheapest plan by scanned slots is taken.
+                const int64_t rrow = A.G.row[root];
+                const int rdeg = vis_deg(A.G, root, rrow, g);
+                const bool rootDown = (W.st[root] & SBC_STEP_MASK) != 0;
+                long long push_cost = 0, mixed_cost = 0;
+                double root_sum = 0.0;
+                const int qbase = sm.st;  // free tail of the same-level queue holds the two lists
+                for (int i = threadIdx.x; i < nn1 + nn2; i += NT) {
+                    const int x = i < nn1 ? nl1[i] : nl2[i - nn1];
+                    double wn, wd;
+                    commit(x, wn, wd);
+                    W.acc[x] = wn;
+                    W.dp[x] = (int64_t)__double_as_longlong(wd);
+                    const int dx = vis_deg(A.G, x, A.G.row[x], g);
+                    push_cost += dx;
+                    if (L == 1) {
+                        root_sum += (rootDown || (root == a && x == b)) ? wn : wd;
+                    } else if (L == 2) {
+                        atomicOr(&W.bits[x >> 5], 1u << (x & 31));
+                        if ((long long)dx > (long long)kProbeRatio * rdeg) {
+                            W.qs[nv - 1 - atomicAdd(&sm.nprobe, 1)] = x;
+                            mixed_cost += (long long)kProbeRatio * rdeg;
+                        } else {
+                            W.qs[qbase + atomicAdd(&sm.nscan, 1)] = x;
+                            mixed_cost += dx;
                         }
                     }
-                    atomicAdd(&W.acc[k], sm.wd[j] - sm.wn[j]);
-                },
-                NoPost());
-            const int same_hi = sm.st;
-            lb_walk<NT, true, ILP>(A.G, g, D, D8, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo, same_hi - same_lo, sm.lb,
-                        prep_div, [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
-            probe_diverted();
+                }
+                block_sum3<NT>(push_cost, mixed_cost, root_sum, sm.part);
+                if (threadIdx.x == 0) {
+                    sm.lb.walked_v += (unsigned)(nn1 + nn2);
+                    sm.lb.walked_e += (unsigned long long)push_cost;
+                }
+                if (L == 1) {
+                    if (threadIdx.x == 0 && nn1 + nn2 > 0) {
+                        W.acc[root] += root_sum;
+                        if (!rootDown) {
+                            int old = atomicOr(&W.st[root], SBC_ASC);
+                            if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = root;
+                        }
+                    }
+                    __syncthreads();
+                } else if (L == 2 && nn1 + nn2 > 0) {
+                    if (pull2_cost < 0) {
+                        long long c = 0;
+                        for (int i = threadIdx.x; i < rdeg; i += NT) {
+                            const int y = A.G.col[rrow + i];
+                            c += vis_deg(A.G, y, A.G.row[y], g);
+                        }
+                        pull2_cost = block_sum<NT>(c, sm.part);
+                    }
+                    if (pull2_cost < mixed_cost) {
+                        pull_walk(A.G.col + rrow, rdeg);
+                    } else {
+                        const int nscan = sm.nscan, nprobe = sm.nprobe;
+                        lb_walk<NT, false, ILP>(A.G, g, D, D8, W.qs + qbase, nscan, nullptr, 0, sm.lb, prep_loaded,
+                                           [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
+                        probe_parents(W.qs + nv - nprobe, nprobe, A.G.col + rrow, rdeg, false);
+                    }
+                    for (int i = threadIdx.x; i < nn1 + nn2; i += NT) {
+                        const int x = i < nn1 ? nl1[i] : nl2[i - nn1];
+                        W.bits[x >> 5] = 0u;  // words hold only this level's marks
+                    }
+                    __syncthreads();
+                }
+            }
         }
         ua_lo = next_lo;
         ua_hi = sm.at;
