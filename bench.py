@@ -51,10 +51,11 @@ def parse():
     p.add_argument("--serve-max-batch", type=int, default=1024)
     p.add_argument("--serve-budget-gb", type=float, default=150.0)
     p.add_argument("--plain-requests", type=int, default=10000, help="serve16: requests on the plain path")
-    p.add_argument("--batch", type=int, default=64)
+    p.add_argument("--batch", type=int, default=0,
+                   help="insertions per batch (0: 256 on rmat20, whose config fixes none; 64 elsewhere)")
     p.add_argument("--group-batch", type=int, default=16,
                    help="rmat_group64: insertions per graph per step (64 graphs per step)")
-    p.add_argument("--plain", type=int, default=16, help="insertions timed on the plain one-at-a-time path")
+    p.add_argument("--plain", type=int, default=128, help="insertions timed on the plain one-at-a-time path")
     p.add_argument("--cpu-roots", type=int, default=0, help="roots in the CPU sample (0 = 2 x host threads)")
     p.add_argument("--cpu-insertions", type=int, default=16)
     p.add_argument("--no-cpu", action="store_true")
@@ -587,7 +588,7 @@ def run_ours(args):
     lib = native.load()
     lib.sbc_set_device(local if world > 1 else 0)
 
-    B = args.batch
+    B = args.batch or (256 if args.workload == "rmat20" else 64)
     # warm-up, the timed `value` pass, then a second pass with per-launch events for the roofline
     n_dev = (args.warmup + 2 * args.steps) * B
     n_e2e = 0 if args.no_e2e else (1 + args.steps) * B
