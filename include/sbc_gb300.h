@@ -162,6 +162,8 @@ int sbc_set_graph_capture(sbc_forest *f, int on);
  * shape index (may be NULL).  The copy needs 21 B per root per vertex; when
  * that does not fit in half the free memory a prefix of the roots is timed. */
 int sbc_forest_set_variant(sbc_forest *f, int variant);
+/* The forest's roots in creation order: roots[nk]. */
+int sbc_forest_roots(const sbc_forest *f, int64_t *roots);
 int sbc_forest_variant(const sbc_forest *f, int *variant);
 int sbc_forest_autotune(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, int reps, int *chosen,
                         double *ms, int ms_len);
@@ -290,7 +292,8 @@ int sbc_server_set_max_inflight(sbc_server *s, int max_inflight);
  * update launch shape by size.  *id is its index (0, 1, ...). */
 int sbc_server_add_graph(sbc_server *s, int64_t nv, const int64_t *off, const int64_t *adj, int64_t nk,
                          const int64_t *roots, int variant, int *id);
-/* state: 0 waiting for admission, 1 admitted, 2 released. */
+/* state: 0 waiting for admission, 1 admitted, 2 released, 3 evicted (its
+ * forest checkpointed in host memory, waiting to be admitted again). */
 int sbc_server_graph_info(sbc_server *s, int id, int *state, int64_t *footprint_bytes, int64_t *completed,
                           int64_t *batches);
 /* One insertion request (arrival time = now).  Thread-safe. */
@@ -307,7 +310,14 @@ const char *sbc_server_error(sbc_server *s);
 /* Free graph id's device memory once its queue is empty (waiting graphs may
  * then be admitted); later requests for it are refused. */
 int sbc_server_release(sbc_server *s, int id);
-/* Results of an idle admitted graph (any pointer may be NULL):
+/* Evict graph id once no batch of it is on the device: its forest is
+ * checkpointed into host memory (sbc_checkpoint_take), its device memory
+ * freed, and it joins the end of the admission queue; requests for it keep
+ * queueing.  When it fits again it is restored from the checkpoint (no static
+ * init) and its queued requests run.  Results equal never evicting it. */
+int sbc_server_evict(sbc_server *s, int id);
+/* Results of an idle admitted graph, or of an evicted one with no queued
+ * requests (from its checkpoint); any pointer may be NULL:
  * dist[nk][nv], sigma[nk][nv], bc[nv]. */
 int sbc_server_read(sbc_server *s, int id, int32_t *dist, int64_t *sigma, double *bc);
 int sbc_server_get_stats(sbc_server *s, sbc_server_stats *stats, int reset);
@@ -344,6 +354,29 @@ int sbc_sync(sbc_forest *f);
  * (any pointer may be NULL); `scanned` is the adjacency slots actually read. */
 int sbc_read_counters(sbc_forest *f, int64_t *vertices, int64_t *edges, int64_t *case1, int64_t *case2,
                       int64_t *scanned);
+
+/* ---- forest checkpoints ---------------------------------------------------
+ * No counterpart in the reference (its forest lives in host records for the
+ * life of the process; STINGER's save/open, src/stinger/stinger.c:1808,1936,
+ * stores the graph alone).  A checkpoint holds the graph's live adjacency as a
+ * CSR, the roots, every root's dist / sigma / delta row and BC, in host
+ * memory.  Restoring builds a new graph and forest in exactly that state with
+ * no static init (one-byte distances, level histograms and rosters are derived
+ * from dist on the device); the restored forest continues where the saved one
+ * stood.  All synchronous. */
+typedef struct sbc_checkpoint sbc_checkpoint;
+int sbc_checkpoint_take(sbc_forest *f, sbc_checkpoint **out);
+/* variant -1: the default update launch shape. */
+int sbc_checkpoint_restore(const sbc_checkpoint *c, int variant, sbc_graph **g, sbc_forest **f);
+/* File form: a 40-byte header ("SBCCKPT1", version 1, nv, nk, ne), then off,
+ * adj (int32), roots, bc, dist, sigma, delta, little-endian. */
+int sbc_checkpoint_save(const sbc_checkpoint *c, const char *path);
+int sbc_checkpoint_load(const char *path, sbc_checkpoint **out);
+/* nv, nk, directed adjacency entries, host bytes held (any may be NULL). */
+int sbc_checkpoint_info(const sbc_checkpoint *c, int64_t *nv, int64_t *nk, int64_t *ne, int64_t *bytes);
+/* The saved state: dist[nk][nv], sigma[nk][nv], bc[nv] (any may be NULL). */
+int sbc_checkpoint_read(const sbc_checkpoint *c, int32_t *dist, int64_t *sigma, double *bc);
+int sbc_checkpoint_free(sbc_checkpoint *c);
 
 /* ---- state read-back (synchronous) ------------------------------------- */
 

@@ -556,6 +556,20 @@ int get_rows(sbc_forest* f, const T* base, int64_t r0, int64_t nr, T* out)
 
 }  // namespace
 
+namespace sbc {
+
+int report_error(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    return fail(code, "%s", buf);
+}
+
+}  // namespace sbc
+
 extern "C" {
 
 const char* sbc_last_error(void) { return t_err.c_str(); }
@@ -961,6 +975,13 @@ int sbc_set_graph_capture(sbc_forest* f, int on)
 {
     if (!f) return fail(SBC_ERR_ARG, "sbc_set_graph_capture: null");
     f->use_graphs = on != 0;
+    return SBC_OK;
+}
+
+int sbc_forest_roots(const sbc_forest* f, int64_t* roots)
+{
+    if (!f || !roots) return fail(SBC_ERR_ARG, "sbc_forest_roots: null");
+    std::copy(f->h_roots.begin(), f->h_roots.end(), roots);
     return SBC_OK;
 }
 

@@ -354,6 +354,8 @@ int update_variant_count();
 int update_default_variant();
 int update_variant_threads(int v);
 int update_workers_per_sm(int v);
+// Sets the calling thread's sbc_last_error() message and returns code.
+int report_error(int code, const char* fmt, ...);
 cudaError_t launch_static(sbc_forest* f);
 // Classify + cull + update for insertions already staged in g->d_ins
 // (u, v, ok rows).  `all_visible` ignores the per-slot sequence numbers.

@@ -18,6 +18,10 @@
 //               the graph's next batch (continuous batching).
 //   completion  a host callback queued behind each batch stamps its completion
 //               time; latency is completion minus the request's arrival time.
+//   eviction    an evicted graph's forest is checkpointed into host memory and
+//               its device memory freed; it rejoins the admission queue and,
+//               once it fits, is restored from the checkpoint (no static init)
+//               with the requests that queued meanwhile.
 // Per-graph order is preserved and results do not depend on how requests are
 // grouped into batches, so each graph ends exactly where applying its stream
 // alone ends.
@@ -44,7 +48,7 @@ struct Req {
     double t_arrival;  // seconds since the server's epoch
 };
 
-enum GraphState { WAITING = 0, ADMITTED = 1, RELEASED = 2 };
+enum GraphState { WAITING = 0, ADMITTED = 1, RELEASED = 2, EVICTED = 3 };
 
 struct ServerGraph {
     int id = 0;
@@ -54,6 +58,8 @@ struct ServerGraph {
     int64_t footprint = 0;
     GraphState state = WAITING;
     bool release_requested = false;
+    bool evict_requested = false;
+    sbc_checkpoint* ckpt = nullptr;  // host copy of an evicted graph's forest
     sbc_graph* g = nullptr;
     sbc_forest* f = nullptr;
     std::deque<Req> pending;
@@ -62,7 +68,7 @@ struct ServerGraph {
     bool done = false;        // set by the completion callback
     double t_done = 0.0;
     std::vector<Req> batch;   // requests of the batch in flight
-    int64_t submitted = 0, completed = 0, batches = 0;
+    int64_t submitted = 0, completed = 0, batches = 0, evictions = 0;
 };
 
 }  // namespace
@@ -142,9 +148,18 @@ void CUDART_CB on_ready(void* p)
 int admit(sbc_server* s, ServerGraph* sg)
 {
     int rc = sbc_set_device(s->device);
-    if (!rc) rc = sbc_graph_create(&sg->g, sg->nv, sg->off.data(), sg->adj.data());
-    if (!rc) rc = sbc_forest_create_ex(&sg->f, sg->g, sg->nk, sg->roots.data(), 0, sg->variant);
-    if (!rc) rc = sbc_static_init(sg->f);
+    if (sg->ckpt) {
+        // an evicted graph: restored where it stood
+        if (!rc) rc = sbc_checkpoint_restore(sg->ckpt, sg->variant, &sg->g, &sg->f);
+        if (!rc) {
+            sbc_checkpoint_free(sg->ckpt);
+            sg->ckpt = nullptr;
+        }
+    } else {
+        if (!rc) rc = sbc_graph_create(&sg->g, sg->nv, sg->off.data(), sg->adj.data());
+        if (!rc) rc = sbc_forest_create_ex(&sg->f, sg->g, sg->nk, sg->roots.data(), 0, sg->variant);
+        if (!rc) rc = sbc_static_init(sg->f);
+    }
     if (!rc && cudaLaunchHostFunc(sg->g->stream, on_ready, new DoneArg{s, sg})) rc = SBC_ERR_CUDA;
     return rc;
 }
@@ -169,6 +184,7 @@ bool pending_work(sbc_server* s)
         if (sg->inflight && sg->done) return true;
         if (can_launch && sg->state == ADMITTED && !sg->inflight && !sg->pending.empty()) return true;
         if (sg->state == ADMITTED && sg->release_requested && !sg->inflight && sg->pending.empty()) return true;
+        if (sg->state == ADMITTED && sg->evict_requested && !sg->inflight && sg->ready) return true;
     }
     return !s->waiting.empty() &&
            s->used + s->graphs[s->waiting.front()]->footprint <= s->budget;
@@ -189,7 +205,7 @@ void scheduler(sbc_server* s)
 {
     sbc_set_device(s->device);
     for (;;) {
-        std::vector<ServerGraph*> launch, admit_list, free_list;
+        std::vector<ServerGraph*> launch, admit_list, free_list, evict_list;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv.wait(lk, [&] { return has_work(s); });
@@ -214,6 +230,14 @@ void scheduler(sbc_server* s)
                     sg->state = RELEASED;
                     s->used -= sg->footprint;
                     free_list.push_back(sg);
+                } else if (sg->state == ADMITTED && sg->evict_requested && !sg->inflight && sg->ready) {
+                    // checkpointed below, before any admission of this round
+                    sg->state = EVICTED;
+                    sg->evict_requested = false;
+                    sg->ready = false;
+                    s->used -= sg->footprint;
+                    s->waiting.push_back(sg->id);
+                    evict_list.push_back(sg);
                 }
             }
             while (!s->waiting.empty() && s->used + s->graphs[s->waiting.front()]->footprint <= s->budget) {
@@ -245,6 +269,30 @@ void scheduler(sbc_server* s)
         }
         // CUDA work outside the lock (completion callbacks take the lock)
         for (ServerGraph* sg : free_list) release_device(sg);
+        for (ServerGraph* sg : evict_list) {
+            const int rc = sbc_checkpoint_take(sg->f, &sg->ckpt);
+            if (rc) {
+                // the graph stays resident (and counted) if its state cannot be saved
+                std::lock_guard<std::mutex> lk(s->mu);
+                if (s->error.empty()) s->error = std::string("eviction: ") + sbc_last_error();
+                s->waiting.erase(std::remove(s->waiting.begin(), s->waiting.end(), sg->id), s->waiting.end());
+                admit_list.erase(std::remove(admit_list.begin(), admit_list.end(), sg), admit_list.end());
+                s->used += sg->footprint;
+                sg->state = ADMITTED;
+                sg->ready = true;
+                continue;
+            }
+            int64_t ne = 0, nk = 0;
+            sbc_checkpoint_info(sg->ckpt, nullptr, &nk, &ne, nullptr);
+            release_device(sg);
+            int sm_count = 0;
+            cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, s->device);
+            std::lock_guard<std::mutex> lk(s->mu);
+            const int64_t fp = footprint(sg->nv, ne, nk, sg->variant, sm_count);  // the graph has grown
+            if (sg->state == ADMITTED) s->used += fp - sg->footprint;  // re-admitted in this round
+            sg->footprint = fp;
+            sg->evictions++;
+        }
         for (ServerGraph* sg : admit_list) {
             int rc = admit(s, sg);
             if (rc) {
@@ -320,6 +368,8 @@ int sbc_server_destroy(sbc_server* s)
     for (auto& p : s->graphs) {
         if (p->g) cudaStreamSynchronize(p->g->stream);
         release_device(p.get());
+        sbc_checkpoint_free(p->ckpt);
+        p->ckpt = nullptr;
     }
     delete s;
     return SBC_OK;
@@ -441,11 +491,28 @@ int sbc_server_release(sbc_server* s, int id)
         if (id < 0 || id >= (int)s->graphs.size()) return SBC_ERR_ARG;
         ServerGraph* sg = s->graphs[id].get();
         sg->release_requested = true;
-        if (sg->state == WAITING) {
+        if (sg->state == WAITING || sg->state == EVICTED) {
             s->waiting.erase(std::remove(s->waiting.begin(), s->waiting.end(), id), s->waiting.end());
             sg->state = RELEASED;
             sg->pending.clear();
+            sbc_checkpoint_free(sg->ckpt);
+            sg->ckpt = nullptr;
         }
+    }
+    s->cv.notify_all();
+    return SBC_OK;
+}
+
+int sbc_server_evict(sbc_server* s, int id)
+{
+    if (!s) return SBC_ERR_ARG;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (id < 0 || id >= (int)s->graphs.size()) return SBC_ERR_ARG;
+        ServerGraph* sg = s->graphs[id].get();
+        if (sg->state == RELEASED || sg->release_requested) return SBC_ERR_STATE;
+        if (sg->state != ADMITTED) return SBC_OK;  // not on the device
+        sg->evict_requested = true;
     }
     s->cv.notify_all();
     return SBC_OK;
@@ -459,7 +526,10 @@ int sbc_server_read(sbc_server* s, int id, int32_t* dist, int64_t* sigma, double
         std::lock_guard<std::mutex> lk(s->mu);
         if (id < 0 || id >= (int)s->graphs.size()) return SBC_ERR_ARG;
         sg = s->graphs[id].get();
-        if (sg->state != ADMITTED || sg->inflight || !sg->pending.empty() || !sg->f) return SBC_ERR_STATE;
+        if (sg->state == EVICTED && sg->pending.empty() && sg->ckpt)
+            return sbc_checkpoint_read(sg->ckpt, dist, sigma, bc);  // the host copy is the state
+        if (sg->state != ADMITTED || sg->inflight || !sg->pending.empty() || !sg->f || sg->evict_requested)
+            return SBC_ERR_STATE;
     }
     sbc_set_device(s->device);
     int rc = sbc_sync(sg->f);
@@ -481,7 +551,7 @@ int sbc_server_get_stats(sbc_server* s, sbc_server_stats* st, int reset)
     st->bytes_admitted = s->used;
     for (auto& p : s->graphs) {
         if (p->state == ADMITTED) st->graphs_admitted++;
-        if (p->state == WAITING) st->graphs_waiting++;
+        if (p->state == WAITING || p->state == EVICTED) st->graphs_waiting++;
     }
     std::vector<double> l = s->lat_us;
     if (!l.empty()) {

@@ -145,6 +145,15 @@ def load(path: str = LIB_PATH):
         "sbc_server_drain": (C.c_int, [_vp]),
         "sbc_server_error": (C.c_char_p, [_vp]),
         "sbc_server_release": (C.c_int, [_vp, C.c_int]),
+        "sbc_server_evict": (C.c_int, [_vp, C.c_int]),
+        "sbc_checkpoint_take": (C.c_int, [_vp, C.POINTER(_vp)]),
+        "sbc_checkpoint_restore": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp)]),
+        "sbc_checkpoint_save": (C.c_int, [_vp, C.c_char_p]),
+        "sbc_checkpoint_load": (C.c_int, [C.c_char_p, C.POINTER(_vp)]),
+        "sbc_checkpoint_info": (C.c_int, [_vp, _i64p, _i64p, _i64p, _i64p]),
+        "sbc_checkpoint_read": (C.c_int, [_vp, _i32p, _i64p, _f64p]),
+        "sbc_checkpoint_free": (C.c_int, [_vp]),
+        "sbc_forest_roots": (C.c_int, [_vp, _i64p]),
         "sbc_server_read": (C.c_int, [_vp, C.c_int, _i32p, _i64p, _f64p]),
         "sbc_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats), C.c_int]),
         "sbc_group_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp), C.c_int]),
@@ -202,6 +211,15 @@ class DeviceGraph:
         self.nv = int(nv)
         self._forests = weakref.WeakSet()
 
+    @classmethod
+    def _adopt(cls, h, nv: int) -> "DeviceGraph":
+        self = cls.__new__(cls)
+        self.lib = load()
+        self.h = h
+        self.nv = int(nv)
+        self._forests = weakref.WeakSet()
+        return self
+
     def remove_directed(self, u: int, v: int) -> int:
         """Remove u -> v: 1 removed, 0 absent, -1 invalid."""
         r = C.c_int(0)
@@ -250,8 +268,80 @@ class DeviceGraph:
             pass
 
 
+class Checkpoint:
+    """sbc_checkpoint: a forest's graph and per-root state in host memory."""
+
+    def __init__(self, h):
+        self.lib = load()
+        self.h = h
+
+    @classmethod
+    def take(cls, forest: "DeviceForest") -> "Checkpoint":
+        h = _vp()
+        _check(load().sbc_checkpoint_take(forest.h, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load(cls, path: str) -> "Checkpoint":
+        h = _vp()
+        _check(load().sbc_checkpoint_load(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    def save(self, path: str):
+        _check(self.lib.sbc_checkpoint_save(self.h, os.fsencode(path)))
+
+    def info(self) -> dict:
+        v = [C.c_int64() for _ in range(4)]
+        _check(self.lib.sbc_checkpoint_info(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("nv", "nk", "ne", "bytes"), [x.value for x in v]))
+
+    def read(self):
+        """(dist [nk][nv] int32, sigma [nk][nv] int64, bc [nv] float64) as saved."""
+        i = self.info()
+        dist = np.zeros((i["nk"], i["nv"]), dtype=np.int32)
+        sigma = np.zeros((i["nk"], i["nv"]), dtype=np.int64)
+        bc = np.zeros(i["nv"], dtype=np.float64)
+        _check(self.lib.sbc_checkpoint_read(self.h, dist.ctypes.data_as(_i32p), p64(sigma),
+                                            bc.ctypes.data_as(_f64p)))
+        return dist, sigma, bc
+
+    def restore(self, variant: int = -1):
+        """A new (DeviceGraph, DeviceForest) in the saved state, no static init."""
+        g, f = _vp(), _vp()
+        _check(self.lib.sbc_checkpoint_restore(self.h, int(variant), C.byref(g), C.byref(f)))
+        dg = DeviceGraph._adopt(g, self.info()["nv"])
+        nk = self.info()["nk"]
+        roots = np.zeros(nk, dtype=np.int64)
+        _check(self.lib.sbc_forest_roots(f, p64(roots)))
+        return dg, DeviceForest._adopt(f, dg, roots)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sbc_checkpoint_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class DeviceForest:
     """sbc_forest: per-root dist/sigma/delta and BC on the device."""
+
+    @classmethod
+    def _adopt(cls, h, graph: "DeviceGraph", roots) -> "DeviceForest":
+        self = cls.__new__(cls)
+        self.lib = load()
+        self.graph = graph
+        self.roots = _a64(roots)
+        self.h = h
+        self.nv = graph.nv
+        self.nk = int(self.roots.size)
+        graph._forests.add(self)
+        self._groups = weakref.WeakSet()
+        return self
 
     def __init__(self, graph: DeviceGraph, roots, workers: int = 0, variant: int = -1):
         self.lib = load()
@@ -598,7 +688,7 @@ class DeviceServer:
         fp, done, nb = C.c_int64(0), C.c_int64(0), C.c_int64(0)
         self._rc(self.lib.sbc_server_graph_info(self.h, int(gid), C.byref(st), C.byref(fp), C.byref(done),
                                                 C.byref(nb)))
-        return {"state": ("waiting", "admitted", "released")[st.value], "footprint": fp.value,
+        return {"state": ("waiting", "admitted", "released", "evicted")[st.value], "footprint": fp.value,
                 "completed": done.value, "batches": nb.value}
 
     def submit(self, gid: int, u: int, v: int):
@@ -620,6 +710,11 @@ class DeviceServer:
 
     def release(self, gid: int):
         self._rc(self.lib.sbc_server_release(self.h, int(gid)))
+
+    def evict(self, gid: int):
+        """Checkpoint graph gid into host memory and free its device memory
+        once no batch of it is on the device; it is restored when it fits."""
+        self._rc(self.lib.sbc_server_evict(self.h, int(gid)))
 
     def read(self, gid: int):
         nv, nk = self._shape[gid]

@@ -131,3 +131,48 @@ def test_drain_waits_for_static_init_without_requests(sbc_lib, mix):
         d, s, b = srv.read(i)
         assert (d[np.arange(len(graphs[i][1])), graphs[i][1]] == 0).all()  # each root at level 0
     srv.close()
+
+
+@pytest.mark.timeout(300)
+def test_eviction_and_restore(sbc_lib, mix):
+    """A budget that holds one graph at a time: graph 0 serves the first half
+    of its stream and is evicted (checkpointed into host memory), so graph 1
+    is admitted; graph 0 reads back from its checkpoint, queues the second
+    half meanwhile, and once graph 1 is released is restored (no static init)
+    and runs what queued.  Both graphs end at their references."""
+    graphs, gid, pairs, t, refs = mix
+    probe = native.DeviceServer(budget_bytes=1 << 40, max_batch=64)
+    fps = [probe.graph_info(probe.add_graph(g, roots))["footprint"] for g, roots in graphs[:2]]
+    probe.close()
+    budget = max(fps) * 3 // 2
+    assert fps[0] + fps[1] > budget
+    srv = native.DeviceServer(budget_bytes=budget, max_batch=64)
+    a = srv.add_graph(*graphs[0])
+    b = srv.add_graph(*graphs[1])
+    mine_a, mine_b = pairs[gid == 0], pairs[gid == 1]
+    half = len(mine_a) // 2
+    for u, v in mine_a[:half]:
+        srv.submit(a, int(u), int(v))
+    for u, v in mine_b:
+        srv.submit(b, int(u), int(v))
+    srv.drain()
+    assert srv.graph_info(a)["state"] == "admitted" and srv.graph_info(b)["state"] == "waiting"
+    partial = srv.read(a)
+    srv.evict(a)
+    srv.drain()
+    assert srv.graph_info(a)["state"] == "evicted"
+    assert srv.graph_info(b)["state"] == "admitted"
+    for x, y in zip(srv.read(a), partial):  # from the checkpoint: the state at eviction
+        np.testing.assert_array_equal(x, y)
+    for u, v in mine_a[half:]:
+        srv.submit(a, int(u), int(v))
+    srv.drain()
+    assert srv.graph_info(a)["state"] == "evicted"  # does not fit beside graph 1
+    _check(srv.read(b), refs[1])
+    srv.release(b)
+    srv.drain()
+    assert srv.graph_info(a)["state"] == "admitted"
+    assert srv.graph_info(a)["completed"] == len(mine_a)
+    _check(srv.read(a), refs[0])
+    assert srv.stats()["bytes_admitted"] <= budget
+    srv.close()
