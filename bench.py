@@ -611,7 +611,9 @@ def run_ours(args):
         all_roots = G.pick_roots(g.nv, min(g.nv, k_rank * world), seed=3)
         roots = shard_roots(all_roots, rank, world)
     gen_s = time.time() - t0
+    t0 = time.time()
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    build_s = time.time() - t0
     f = native.DeviceForest(dg, roots, workers=args.workers, variant=args.variant)
     dg.reserve(ins_all)  # slack for every insertion of the run, planned before timing
 
@@ -803,6 +805,7 @@ def run_ours(args):
                        "l2": f"per-root state {info['bytes'] / 1e9:.1f} GB on device >> 129 MB L2; no flush",
                        "workers": info["workers"], "variant": f.variant, "autotune": tuned,
                        "static_init_s": static_s,
+                       "graph_build_s": build_s,
                        "generate_s": gen_s,
                        "timing": "value: K batches replayed from a captured CUDA graph, CUDA events on the "
                                  "library stream; roofline: the next K batches launched directly with events "

@@ -95,6 +95,17 @@ int sbc_graph_repacks(const sbc_graph *g, int64_t *count);
 /* Copy the live adjacency back as CSR: off[nv+1]; adj may be NULL to query
  * off[nv] first.  Neighbour order is storage order. */
 int sbc_graph_to_csr(sbc_graph *g, int64_t *off, int64_t *adj);
+/* DIMACS graph files (ParseDimacsGraph, src/sbcMain_utils.c:382-422): header
+ * "NV NE", then line u (u = 1, 2, ...) lists vertex u's neighbours, 1-based
+ * ids used as they stand, reading stopping at a line's first non-integer
+ * token.  The CSR has nv = NV + 1 vertices (vertex 0 isolated) and ne entries.
+ * Parsed by all host threads; more lines than NV or an id outside 0..NV is an
+ * error.  *off (nv+1) and *adj (ne) are malloc'd: release them with sbc_free.
+ * No device needed. */
+int sbc_dimacs_read(const char *path, int64_t *nv, int64_t *ne, int64_t **off, int64_t **adj);
+void sbc_free(void *p);
+/* sbc_dimacs_read + sbc_graph_create (nv, ne may be NULL). */
+int sbc_graph_create_dimacs(sbc_graph **out, const char *path, int64_t *nv, int64_t *ne);
 
 /* ---- forest ------------------------------------------------------------- */
 

@@ -151,6 +151,13 @@ void CreateStingerFromCSR(csrGraph *csr, struct stinger **stingerGraph);
 csrGraph *CreateEmptyUndirectedCSR(int64_t NV, int64_t NE);
 csrGraph *CreateEmptyDirectedCSR(int64_t NV, int64_t NE);
 void FreeCSR(csrGraph *graph);
+/* src/streamingbc.h:84 (src/sbcMain_utils.c:382-422): a DIMACS .graph file
+ * into a new device graph; *NV counts the unused vertex 0 (header NV + 1) and
+ * *NE is the header's NE doubled, as in the reference.  The file is parsed by
+ * all host threads and the adjacency built on the device; on failure
+ * *stingerGraph is NULL and sbc_last_error() says why (the reference would
+ * crash). */
+void ParseDimacsGraph(char initial_graph_name[1024], struct stinger **stingerGraph, int64_t *NV, int64_t *NE);
 /* src/sbcMain_utils.c:425-456: identity when NK == NV, else NK distinct
  * vertices drawn with rand() (seed with srand). */
 void PickRoots(int64_t *rootArrayForApproximation, int64_t NK, int64_t NV);

@@ -620,14 +620,6 @@ int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int6
     }
     g->h_row[nv] = total;
     g->total_cap = total;
-    // Each vertex's initial neighbours are stored sorted, so adjacency can be
-    // tested by binary search (insertions later append an unsorted tail).
-    std::vector<int32_t> col(total > 0 ? total : 1, 0);
-    for (int64_t v = 0; v < nv; ++v) {
-        int32_t* dst = col.data() + g->h_row[v];
-        for (int64_t e = off[v]; e < off[v + 1]; ++e) dst[e - off[v]] = (int32_t)adj[e];
-        std::sort(dst, dst + (off[v + 1] - off[v]));
-    }
 
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) ||
@@ -644,10 +636,23 @@ int sbc_graph_create(sbc_graph** out, int64_t nv, const int64_t* off, const int6
         (nv && (e = cudaMemcpy(g->d_deg0, deg.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
         (nv && (e = cudaMemcpy(g->d_nsort, deg.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
         (nv && (e = cudaMemcpy(g->d_cap, g->h_cap.data(), sizeof(int32_t) * nv, cudaMemcpyHostToDevice))) ||
-        (e = cudaMemcpy(g->d_col, col.data(), sizeof(int32_t) * col.size(), cudaMemcpyHostToDevice)) ||
-        (e = cudaMemset(g->d_seq, 0, sizeof(int32_t) * col.size())) || (e = cudaMemset(g->d_err, 0, 2 * sizeof(int)))) {
+        (e = cudaMemset(g->d_col, 0, sizeof(int32_t) * std::max<int64_t>(total, 1))) ||
+        (e = cudaMemset(g->d_seq, 0, sizeof(int32_t) * std::max<int64_t>(total, 1))) ||
+        (e = cudaMemset(g->d_err, 0, 2 * sizeof(int)))) {
         sbc_graph_destroy(g);
         return cuda_fail(e, "sbc_graph_create upload");
+    }
+    // Each vertex's initial neighbours are stored sorted, so adjacency can be
+    // tested by binary search (insertions later append an unsorted tail); the
+    // scatter into the slack layout and the sort run on the device.
+    {
+        int sm_count = 0;
+        cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if ((e = sbc::build_adjacency(nv, off, adj, g->d_row, g->d_deg, deg, g->d_col, std::max(sm_count, 1),
+                                      g->stream))) {
+            sbc_graph_destroy(g);
+            return cuda_fail(e, "sbc_graph_create adjacency build");
+        }
     }
     int rc = ensure_staging(g, 64);
     if (rc) {

@@ -356,6 +356,12 @@ int update_variant_threads(int v);
 int update_workers_per_sm(int v);
 // Sets the calling thread's sbc_last_error() message and returns code.
 int report_error(int code, const char* fmt, ...);
+// Scatters the caller's host CSR into the device slack layout (d_row, d_deg
+// already set; deg = the live degrees) and sorts every vertex's list on the
+// device.  Synchronous on s.
+cudaError_t build_adjacency(int64_t nv, const int64_t* off, const int64_t* adj, const int64_t* d_row,
+                            const int32_t* d_deg, const std::vector<int32_t>& deg, int32_t* d_col, int sm_count,
+                            cudaStream_t s);
 cudaError_t launch_static(sbc_forest* f);
 // Classify + cull + update for insertions already staged in g->d_ins
 // (u, v, ok rows).  `all_visible` ignores the per-slot sequence numbers.

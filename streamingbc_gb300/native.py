@@ -154,6 +154,9 @@ def load(path: str = LIB_PATH):
         "sbc_checkpoint_read": (C.c_int, [_vp, _i32p, _i64p, _f64p]),
         "sbc_checkpoint_free": (C.c_int, [_vp]),
         "sbc_forest_roots": (C.c_int, [_vp, _i64p]),
+        "sbc_dimacs_read": (C.c_int, [C.c_char_p, _i64p, _i64p, C.POINTER(_i64p), C.POINTER(_i64p)]),
+        "sbc_free": (None, [_vp]),
+        "sbc_graph_create_dimacs": (C.c_int, [C.POINTER(_vp), C.c_char_p, _i64p, _i64p]),
         "sbc_server_read": (C.c_int, [_vp, C.c_int, _i32p, _i64p, _f64p]),
         "sbc_server_get_stats": (C.c_int, [_vp, C.POINTER(ServerStats), C.c_int]),
         "sbc_group_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(_vp), C.c_int]),
@@ -212,6 +215,16 @@ class DeviceGraph:
         self._forests = weakref.WeakSet()
 
     @classmethod
+    def from_dimacs(cls, path: str) -> "DeviceGraph":
+        """A device graph from a DIMACS .graph file (parsed by all host
+        threads, adjacency built on the device)."""
+        lib = load()
+        h = _vp()
+        nv = C.c_int64(0)
+        _check(lib.sbc_graph_create_dimacs(C.byref(h), os.fsencode(path), C.byref(nv), None))
+        return cls._adopt(h, nv.value)
+
+    @classmethod
     def _adopt(cls, h, nv: int) -> "DeviceGraph":
         self = cls.__new__(cls)
         self.lib = load()
@@ -266,6 +279,23 @@ class DeviceGraph:
             self.close()
         except Exception:
             pass
+
+
+def read_dimacs(path: str):
+    """Parse a DIMACS .graph file with the library's threaded parser (the
+    reference's ParseDimacsGraph reading: vertex 0 isolated, line u = vertex
+    u).  Returns (nv, off int64[nv+1], adj int64[ne]).  Needs no GPU."""
+    lib = load()
+    nv, ne = C.c_int64(0), C.c_int64(0)
+    po, pa = _i64p(), _i64p()
+    _check(lib.sbc_dimacs_read(os.fsencode(path), C.byref(nv), C.byref(ne), C.byref(po), C.byref(pa)))
+    try:
+        off = np.ctypeslib.as_array(po, shape=(nv.value + 1,)).copy()
+        adj = np.ctypeslib.as_array(pa, shape=(max(ne.value, 1),))[:ne.value].copy()
+    finally:
+        lib.sbc_free(C.cast(po, _vp))
+        lib.sbc_free(C.cast(pa, _vp))
+    return nv.value, off, adj
 
 
 class Checkpoint:
