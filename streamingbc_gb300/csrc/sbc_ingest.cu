@@ -141,6 +141,7 @@ cudaError_t build_adjacency(int64_t nv, const int64_t* off, const int64_t* adj, 
     int64_t tmp_total = 0;
     for (int64_t v = 0; v < nv; ++v) {
         if (deg[v] <= 1) continue;
+        if (deg[v] > (1 << 30)) return cudaErrorInvalidValue;  // the sort pads lists to a power of two in int
         if (deg[v] <= 32) {
             shortl.push_back((int32_t)v);
         } else {
