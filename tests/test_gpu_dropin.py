@@ -100,3 +100,52 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case, port
     assert vdeg == (len(nb), 0)
     assert bc_err(bc["vertex"], o.bc()) <= BC_RTOL
     o.close()
+
+
+@pytest.fixture(scope="module")
+def dimacs_driver(tmp_path_factory, sbc_lib):
+    d = tmp_path_factory.mktemp("dimacs")
+    exe = d / "dimacs_driver"
+    libdir = os.path.dirname(native.LIB_PATH)
+    r = subprocess.run(["gcc", "-std=c99", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(HERE, "c", "dimacs_driver.c"), "-o", str(exe), "-L", libdir,
+                        "-lsbc_gb300", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_dimacs_driver_compiles(dimacs_driver):
+    assert os.path.exists(dimacs_driver)
+
+
+@pytest.mark.gpu
+def test_reference_driver_flow_from_a_dimacs_file(dimacs_driver, tmp_path):
+    """karate written as a DIMACS file and run through the reference driver's
+    flow (ParseDimacsGraph, PickRoots with NK = NV: exact BC, static init,
+    insertions): BC after static init and after every insertion equals the
+    reference's golden vectors (the file's vertex u + 1 is golden vertex u;
+    vertex 0, the unused slot, stays at 0)."""
+    from test_ingest import to_dimacs
+    z = load_golden("karate")
+    n0 = int(z["nv"])
+    graph = tmp_path / "karate.graph"
+    graph.write_text(to_dimacs(n0, z["off"], z["adj"], ne_header=78))
+    ins = z["ins"][:16]
+    insf = tmp_path / "ins.txt"
+    insf.write_text(f"{len(ins)}\n" + "".join(f"{u + 1} {v + 1}\n" for u, v in ins.tolist()))
+    outp = tmp_path / "out.txt"
+    r = subprocess.run([str(dimacs_driver), str(graph), "0", str(insf), str(outp)], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = outp.read_text().split("\n")
+    assert lines[0] == f"nv {n0 + 1} ne 156"
+    bc = {}
+    for line in lines[1:]:
+        if line.startswith("bc "):
+            p = line.split()
+            bc[int(p[1])] = np.array([float(x) for x in p[2:]])
+    assert bc[-1][0] == 0.0
+    assert bc_err(bc[-1][1:], z["bc0"]) <= BC_RTOL
+    for i in range(len(ins)):
+        assert bc[i][0] == 0.0
+        assert bc_err(bc[i][1:], z["bc_trace"][i]) <= BC_RTOL, i
