@@ -523,15 +523,13 @@ def run_group(args):
     if n_e2e:
         base = n_val // B
         grp.insert(batches(base))
-        for _, f in objs:
-            f.bc()
+        grp.bc()
         lat = []
         t1 = time.perf_counter()
         for s in range(base + 1, base + 1 + args.steps):
             ts = time.perf_counter()
             grp.insert(batches(s))
-            for _, f in objs:
-                f.bc()
+            grp.bc()  # every member's BC vector, one wait
             lat.append((time.perf_counter() - ts) * 1e3)
         e2e_s = time.perf_counter() - t1
         nv_sum = sum(g.nv for g, _, _, _ in specs)

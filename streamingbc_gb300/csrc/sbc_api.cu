@@ -1604,8 +1604,35 @@ int sbc_group_destroy(sbc_group* G)
     if (G->ev) cudaEventDestroy(G->ev);
     if (G->t0) cudaEventDestroy(G->t0);
     if (G->t1) cudaEventDestroy(G->t1);
+    if (G->h_bc) cudaFreeHost(G->h_bc);
     if (G->stream) cudaStreamDestroy(G->stream);
     delete G;
+    return SBC_OK;
+}
+
+int sbc_group_get_bc(sbc_group* G, double* bc)
+{
+    int rc = group_check(G);
+    if (rc) return rc;
+    if (!bc) return fail(SBC_ERR_ARG, "sbc_group_get_bc: null");
+    if ((rc = group_after_members(G))) return rc;
+    int64_t total = 0;
+    for (sbc_forest* f : G->members) total += f->nv;
+    if (total > G->h_bc_cap) {
+        if (G->h_bc) cudaFreeHost(G->h_bc);
+        G->h_bc = nullptr;
+        G->h_bc_cap = 0;
+        CK(cudaMallocHost(&G->h_bc, sizeof(double) * std::max<int64_t>(total, 1)));
+        G->h_bc_cap = total;
+    }
+    // one asynchronous copy per member into pinned memory, one wait
+    int64_t o = 0;
+    for (sbc_forest* f : G->members) {
+        CK(cudaMemcpyAsync(G->h_bc + o, f->d_bc, sizeof(double) * f->nv, cudaMemcpyDeviceToHost, G->stream));
+        o += f->nv;
+    }
+    CK(cudaStreamSynchronize(G->stream));
+    memcpy(bc, G->h_bc, sizeof(double) * total);
     return SBC_OK;
 }
 

@@ -295,6 +295,8 @@ struct sbc_group {
     unsigned long long* d_counters = nullptr;  // [SBC_NCOUNTERS]
     cudaEvent_t ev = nullptr;                  // stream hand-off
     cudaEvent_t t0 = nullptr, t1 = nullptr;    // device time of the last batch
+    double* h_bc = nullptr;                    // pinned staging of every member's BC
+    int64_t h_bc_cap = 0;
 };
 
 namespace sbc {

@@ -154,6 +154,7 @@ def load(path: str = LIB_PATH):
         "sbc_checkpoint_read": (C.c_int, [_vp, _i32p, _i64p, _f64p]),
         "sbc_checkpoint_free": (C.c_int, [_vp]),
         "sbc_forest_roots": (C.c_int, [_vp, _i64p]),
+        "sbc_group_get_bc": (C.c_int, [_vp, _f64p]),
         "sbc_dimacs_read": (C.c_int, [C.c_char_p, _i64p, _i64p, C.POINTER(_i64p), C.POINTER(_i64p)]),
         "sbc_free": (None, [_vp]),
         "sbc_graph_create_dimacs": (C.c_int, [C.POINTER(_vp), C.c_char_p, _i64p, _i64p]),
@@ -660,6 +661,13 @@ class DeviceGroup:
         _check(self.lib.sbc_group_autotune(self.h, p64(counts), p64(u), p64(v), int(reps), C.byref(chosen),
                                            ms.ctypes.data_as(_f64p), n.value))
         return chosen.value, ms
+
+    def bc(self) -> list:
+        """Every member's BC vector (one wait for all of them)."""
+        sizes = [f.nv for f in self.forests]
+        out = np.zeros(int(sum(sizes)), dtype=np.float64)
+        _check(self.lib.sbc_group_get_bc(self.h, out.ctypes.data_as(_f64p)))
+        return np.split(out, np.cumsum(sizes)[:-1])
 
     def set_variant(self, variant: int):
         _check(self.lib.sbc_group_set_variant(self.h, int(variant)))

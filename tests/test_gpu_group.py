@@ -56,10 +56,12 @@ def test_group_matches_oracle_per_member(sbc_lib, port_lib):
                 orcs[i].insert(int(u), int(v))
         ms = grp.insert(batches)
         assert ms >= 0.0
+        all_bc = grp.bc()  # every member's BC through one group read
         for i, (_, f) in enumerate(fs):
             assert_levels(f.level64(), orcs[i].level())
             assert_sigma(f.sigma(), orcs[i].sigma(), orcs[i].level())
             assert_bc(f.bc(), orcs[i].bc(), what=f"member {i} bc")
+            np.testing.assert_array_equal(all_bc[i], f.bc())
     assert all(pos[i] == len(specs[i][2]) for i in range(len(specs)))
     grp.close()
     for dg, f in fs:
