@@ -271,8 +271,9 @@ int sbc_group_autotune(sbc_group *G, const int64_t *counts, const int64_t *u, co
                        int *chosen, double *ms, int ms_len);
 int sbc_group_read_counters(sbc_group *G, int64_t *vertices, int64_t *edges, int64_t *case1, int64_t *case2,
                             int64_t *scanned);
-/* Every member's BC vector, concatenated in member order (bc[Σ nv]), after all
- * work queued on the group and its members: one wait for all of them. */
+/* Every member's BC vector, concatenated in the order the members were given
+ * to sbc_group_create (bc[Σ nv]), after all work queued on the group and its
+ * members: one wait for all of them. */
 int sbc_group_get_bc(sbc_group *G, double *bc);
 
 /* ---- serving loop ---------------------------------------------------------

@@ -1625,11 +1625,17 @@ int sbc_group_get_bc(sbc_group* G, double* bc)
         CK(cudaMallocHost(&G->h_bc, sizeof(double) * std::max<int64_t>(total, 1)));
         G->h_bc_cap = total;
     }
-    // one asynchronous copy per member into pinned memory, one wait
-    int64_t o = 0;
-    for (sbc_forest* f : G->members) {
-        CK(cudaMemcpyAsync(G->h_bc + o, f->d_bc, sizeof(double) * f->nv, cudaMemcpyDeviceToHost, G->stream));
-        o += f->nv;
+    // one asynchronous copy per member into pinned memory, one wait; slot s
+    // holds the caller's member order[s], whose vector goes at its offset in
+    // the caller's order
+    const size_t n = G->members.size();
+    std::vector<int64_t> at(n + 1, 0);
+    for (size_t s = 0; s < n; ++s) at[G->order[s] + 1] = G->members[s]->nv;
+    for (size_t i = 0; i < n; ++i) at[i + 1] += at[i];
+    for (size_t s = 0; s < n; ++s) {
+        sbc_forest* f = G->members[s];
+        CK(cudaMemcpyAsync(G->h_bc + at[G->order[s]], f->d_bc, sizeof(double) * f->nv, cudaMemcpyDeviceToHost,
+                           G->stream));
     }
     CK(cudaStreamSynchronize(G->stream));
     memcpy(bc, G->h_bc, sizeof(double) * total);
