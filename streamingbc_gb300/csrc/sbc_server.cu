@@ -270,24 +270,34 @@ void scheduler(sbc_server* s)
         // CUDA work outside the lock (completion callbacks take the lock)
         for (ServerGraph* sg : free_list) release_device(sg);
         for (ServerGraph* sg : evict_list) {
-            const int rc = sbc_checkpoint_take(sg->f, &sg->ckpt);
+            sbc_checkpoint* ck = nullptr;
+            const int rc = sbc_checkpoint_take(sg->f, &ck);
             if (rc) {
                 // the graph stays resident (and counted) if its state cannot be saved
                 std::lock_guard<std::mutex> lk(s->mu);
                 if (s->error.empty()) s->error = std::string("eviction: ") + sbc_last_error();
-                s->waiting.erase(std::remove(s->waiting.begin(), s->waiting.end(), sg->id), s->waiting.end());
-                admit_list.erase(std::remove(admit_list.begin(), admit_list.end(), sg), admit_list.end());
-                s->used += sg->footprint;
-                sg->state = ADMITTED;
+                auto it = std::find(admit_list.begin(), admit_list.end(), sg);
+                if (it != admit_list.end()) {
+                    admit_list.erase(it);  // re-admitted this round: already counted and out of the queue
+                } else {
+                    s->waiting.erase(std::remove(s->waiting.begin(), s->waiting.end(), sg->id), s->waiting.end());
+                    s->used += sg->footprint;
+                }
+                if (sg->state != RELEASED) sg->state = ADMITTED;
                 sg->ready = true;
                 continue;
             }
             int64_t ne = 0, nk = 0;
-            sbc_checkpoint_info(sg->ckpt, nullptr, &nk, &ne, nullptr);
+            sbc_checkpoint_info(ck, nullptr, &nk, &ne, nullptr);
             release_device(sg);
             int sm_count = 0;
             cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, s->device);
             std::lock_guard<std::mutex> lk(s->mu);
+            if (sg->state == RELEASED) {  // released while its checkpoint was being taken
+                sbc_checkpoint_free(ck);
+                continue;
+            }
+            sg->ckpt = ck;  // published under the lock: readers and release see it whole
             const int64_t fp = footprint(sg->nv, ne, nk, sg->variant, sm_count);  // the graph has grown
             if (sg->state == ADMITTED) s->used += fp - sg->footprint;  // re-admitted in this round
             sg->footprint = fp;
