@@ -274,17 +274,25 @@ void scheduler(sbc_server* s)
             const int rc = sbc_checkpoint_take(sg->f, &ck);
             if (rc) {
                 // the graph stays resident (and counted) if its state cannot be saved
-                std::lock_guard<std::mutex> lk(s->mu);
-                if (s->error.empty()) s->error = std::string("eviction: ") + sbc_last_error();
-                auto it = std::find(admit_list.begin(), admit_list.end(), sg);
-                if (it != admit_list.end()) {
-                    admit_list.erase(it);  // re-admitted this round: already counted and out of the queue
-                } else {
-                    s->waiting.erase(std::remove(s->waiting.begin(), s->waiting.end(), sg->id), s->waiting.end());
-                    s->used += sg->footprint;
+                bool released = false;
+                {
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    if (s->error.empty()) s->error = std::string("eviction: ") + sbc_last_error();
+                    released = sg->state == RELEASED;  // released meanwhile: out of the queue, not counted
+                    if (!released) {
+                        auto it = std::find(admit_list.begin(), admit_list.end(), sg);
+                        if (it != admit_list.end()) {
+                            admit_list.erase(it);  // re-admitted this round: already counted and dequeued
+                        } else {
+                            s->waiting.erase(std::remove(s->waiting.begin(), s->waiting.end(), sg->id),
+                                             s->waiting.end());
+                            s->used += sg->footprint;
+                        }
+                        sg->state = ADMITTED;
+                        sg->ready = true;
+                    }
                 }
-                if (sg->state != RELEASED) sg->state = ADMITTED;
-                sg->ready = true;
+                if (released) release_device(sg);
                 continue;
             }
             int64_t ne = 0, nk = 0;
