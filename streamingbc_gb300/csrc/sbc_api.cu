@@ -867,6 +867,7 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_counters);
     dev_free(f->d_lvlhist);
     dev_free(f->d_mov);
+    dev_free(f->d_wide);
     dev_free(f->d_nmov);
     dev_free(f->d_roster);
     dev_free(f->d_roster_n);

@@ -190,6 +190,7 @@ struct sbc_forest {
     int* d_worklist = nullptr;
     int* d_mov = nullptr;     // [nk] roots a deletion leaves without a parent of the deeper endpoint
     int* d_nmov = nullptr;    // [2]: their count, work counter
+    int* d_wide = nullptr;    // [3 * kWideRecompute]: BFS lengths and level ranges of the wide recompute
     int* d_res = nullptr;     // [1] result of the last edge removal
     int* d_nwork = nullptr;   // [1]
     int* d_counter = nullptr; // [1]
@@ -385,10 +386,12 @@ cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed);
 // Static recompute of the roots listed (device list and count) or, with a
 // null list, of all roots.
 cudaError_t launch_static_list(sbc_forest* f, const int* d_list, const int* d_nlist);
-// Whole-GPU recompute of root row r (level-synchronous, synchronous); used by
-// deletions on graphs of at least kWideRecomputeMinVertices vertices for up to
-// kWideRecompute roots, the static kernel otherwise.
-cudaError_t recompute_root_wide(sbc_forest* f, int r);
+// Whole-GPU recompute of the listed root rows (rows on the host, d_rows the
+// same list on the device), all of them level by level together
+// (level-synchronous, synchronous); used by deletions on graphs of at least
+// kWideRecomputeMinVertices vertices for up to kWideRecompute roots, the
+// static kernel otherwise.
+cudaError_t recompute_roots_wide(sbc_forest* f, const std::vector<int>& rows, const int* d_rows);
 constexpr int kWideRecompute = 64;
 constexpr int64_t kWideRecomputeMinVertices = 32768;
 cudaError_t launch_level_hist_list(sbc_forest* f, const int* d_list, const int* d_nlist);

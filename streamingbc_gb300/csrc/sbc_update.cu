@@ -296,8 +296,7 @@ cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)
         if ((e = cudaMemcpyAsync(rows.data(), f->d_mov, sizeof(int) * nmov, cudaMemcpyDeviceToHost, s)) ||
             (e = cudaStreamSynchronize(s)))
             return e;
-        for (int r : rows)
-            if ((e = recompute_root_wide(f, r))) return e;
+        if ((e = recompute_roots_wide(f, rows, f->d_mov))) return e;
     } else if ((e = launch_static_list(f, f->d_mov, f->d_nmov))) {
         return e;
     }
