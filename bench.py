@@ -63,8 +63,10 @@ def parse():
     p.add_argument("--group-batch", type=int, default=16,
                    help="rmat_group64: insertions per graph per step (64 graphs per step)")
     p.add_argument("--plain", type=int, default=128, help="insertions timed on the plain one-at-a-time path")
-    p.add_argument("--cpu-roots", type=int, default=0, help="roots in the CPU sample (0 = 2 x host threads)")
-    p.add_argument("--cpu-insertions", type=int, default=16)
+    p.add_argument("--cpu-insertions", type=int, default=32,
+                   help="CPU baseline: insertions timed over all K roots with every host thread")
+    p.add_argument("--cpu-insertions-nt1", type=int, default=2,
+                   help="CPU baseline: the next insertions timed with one thread (the reference's NT = 1)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--variant", type=int, default=-1,
@@ -111,6 +113,43 @@ def load_workload(name, count):
         return g, G.pick_roots(g.nv, 256, 2), G.local_insertions(g, max(count, 4096), seed=2)[:count]
     g = G.er(1024, 8192, seed=1)
     return g, G.pick_roots(g.nv, g.nv, 1), G.uniform_insertions(g, count, seed=1)
+
+
+def kernel_source_hash() -> str:
+    """sha256 (first 16 hex digits) of the CUDA sources and headers the
+    library is built from: a committed DRAM-traffic capture counts only for
+    the kernel sources it was taken with."""
+    import glob
+    import hashlib
+    h = hashlib.sha256()
+    csrc = os.path.join(ROOT, "streamingbc_gb300", "csrc")
+    for path in sorted(glob.glob(os.path.join(csrc, "*.cu")) + glob.glob(os.path.join(csrc, "*.cuh")) +
+                       glob.glob(os.path.join(csrc, "*.h"))):
+        h.update(os.path.basename(path).encode())
+        with open(path, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def traffic_estimate(workload, batch, alg_bytes_per_launch):
+    """DRAM bytes per k_update launch: profiles/k_update_<workload>_traffic.json
+    holds one small-case ncu capture (dram__bytes_read.sum +
+    dram__bytes_write.sum) with that launch's algorithmic bytes and the hash of
+    the kernel sources it ran; the ratio is applied to this run's algorithmic
+    bytes.  A capture of other sources, or none, gives null."""
+    path = os.path.join(ROOT, "profiles", f"k_update_{workload}_traffic.json")
+    try:
+        with open(path) as fh:
+            tj = json.load(fh)
+    except (OSError, ValueError):
+        return None, "no capture of this workload"
+    if tj.get("source_hash") != kernel_source_hash():
+        return None, (f"capture in {os.path.basename(path)} was taken with other kernel sources "
+                      f"({tj.get('source_hash')}); not used")
+    ratio = float(tj["dram_bytes_per_launch"]) / float(tj["alg_bytes_per_launch"])
+    return ratio * alg_bytes_per_launch, (f"small-case ncu capture ({tj.get('case')}): DRAM/algorithmic bytes "
+                                          f"{ratio:.3f}, applied to this run's algorithmic bytes; sources "
+                                          f"{tj['source_hash']}")
 
 
 def measured_peak():
@@ -201,27 +240,69 @@ def barrier(world: int):
         dist.barrier()
 
 
-def cpu_sample(g, roots, ins, n_roots, n_ins, threads):
-    """Oracle port (the reference algorithm in C, OpenMP over roots) on a
-    bounded sample: n_roots of the K roots, the first n_ins insertions.
-    Per-insertion time at K roots = per-root part * K/n_roots + BC reduce."""
+def host_avail_bytes() -> int:
+    try:
+        return os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_AVPHYS_PAGES")
+    except (ValueError, OSError):
+        return 8 << 30
+
+
+def cpu_port_time(g, roots, ins, n_all, n_one, threads):
+    """The oracle port -- the reference's COARSE algorithm in C, OpenMP over
+    roots -- over ALL K roots, no extrapolation: static init, then the first
+    n_all insertions of the stream with every host thread, then the next
+    n_one with one thread (the reference's NT = 1).  Each insertion is timed
+    like updateEdgeNEW (src/sbcMain_utils.c:568-571): the per-root updates and
+    the per-thread BC reduce, not the graph insert.  When the K x V forest
+    (24 B per cell) does not fit half the free host memory, roots run in
+    chunks (each chunk a fresh oracle on the same graph and stream): an
+    insertion's time is then the sum of its per-root phase over the chunks
+    plus the BC reduce once."""
     from oracle import oracle as orc
     orc.build()
-    sample_roots = roots[:n_roots]
-    o = orc.PortOracle(g.nv, g.off, g.adj, sample_roots, nthreads=threads)
-    t_static = o.static_timed()
-    per = []
-    for u, v in ins[:n_ins]:
-        tr, tb = o.insert_timed(int(u), int(v))
-        per.append(tr * (len(roots) / n_roots) + tb)
-    o.close()
-    mean = float(np.mean(per))
-    return {"value": 1.0 / mean, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n_roots} of {len(roots)} roots, first {n_ins} insertions; per-insertion per-root time "
-                      f"scaled x{len(roots) / n_roots:g}, BC reduce (O(NV*threads)) added once",
-            "per_insertion_ms": {"mean": mean * 1e3, "p50": float(np.percentile(per, 50)) * 1e3,
-                                 "p99": float(np.percentile(per, 99)) * 1e3},
-            "static_sample_s": t_static}
+    K = len(roots)
+    cell = 24 * g.nv
+    chunk = K
+    while chunk > 1 and chunk * cell * 1.25 > host_avail_bytes() // 2:
+        chunk = (chunk + 1) // 2
+    t_all = np.zeros(n_all)
+    t_one = np.zeros(n_one)
+    static_s = 0.0
+    for c in range(0, K, chunk):
+        o = orc.PortOracle(g.nv, g.off, g.adj, roots[c:c + chunk], nthreads=threads)
+        static_s += o.static_timed()
+        for i, (u, v) in enumerate(ins[:n_all]):
+            tr, tb = o.insert_timed(int(u), int(v))
+            t_all[i] += tr + (tb if c == 0 else 0.0)
+        o.set_threads(1)
+        for i, (u, v) in enumerate(ins[n_all:n_all + n_one]):
+            tr, tb = o.insert_timed(int(u), int(v))
+            t_one[i] += tr + (tb if c == 0 else 0.0)
+        o.close()
+    return {"t_all": t_all, "t_one": t_one, "static_s": static_s, "chunk": chunk}
+
+
+def _lat(ts) -> dict:
+    return {"mean": float(np.mean(ts)) * 1e3, "p50": float(np.percentile(ts, 50)) * 1e3,
+            "p99": float(np.percentile(ts, 99)) * 1e3}
+
+
+def cpu_sample(g, roots, ins, n_all, n_one, threads):
+    """CPU baseline of one forest: the oracle port over all K roots on the
+    first n_all insertions of the stream (all host threads) and the next
+    n_one (one thread)."""
+    r = cpu_port_time(g, roots, ins, n_all, n_one, threads)
+    out = {"value": 1.0 / float(np.mean(r["t_all"])), "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"all {len(roots)} roots (no extrapolation), insertions 1..{n_all} of the stream after static "
+                     f"init, {threads} threads; then insertions {n_all + 1}..{n_all + n_one} with 1 thread; "
+                     f"timed like updateEdgeNEW (per-root updates + BC reduce, graph insert excluded)"
+                     + (f"; roots in chunks of {r['chunk']} to fit host memory" if r["chunk"] < len(roots) else ""),
+           "per_insertion_ms": _lat(r["t_all"]),
+           "static_init_s": r["static_s"]}
+    if n_one:
+        out["nt1"] = {"value": 1.0 / float(np.mean(r["t_one"])), "unit": UNIT, "cores": 1,
+                      "insertions": n_one, "per_insertion_ms": _lat(r["t_one"])}
+    return out
 
 
 GROUP_WORKLOAD = "rmat_group64"
@@ -231,28 +312,19 @@ GROUP_DESC = ("rmat_group64: 64 independent R-MAT graphs, scales uniform in 10..
 
 
 def cpu_sample_group(specs, batch, n_ins, threads):
-    """Oracle port on every graph of the group: min(K, 2*threads) roots and
-    the first n_ins insertions per graph; a group step's CPU time is the sum
-    over graphs of batch x (per-root time x K/n_roots + BC reduce)."""
-    from oracle import oracle as orc
-    orc.build()
+    """Oracle port on every graph of the group, all K roots of each, its
+    first n_ins insertions; a group step's CPU time is the sum over graphs of
+    batch x that graph's mean per-insertion time."""
     total = 0.0
     per_graph = []
     for g, roots, ins, _ in specs:
-        nr = min(len(roots), 2 * threads)
-        o = orc.PortOracle(g.nv, g.off, g.adj, roots[:nr], nthreads=threads)
-        o.static_timed()
-        per = []
-        for u, v in ins[:n_ins]:
-            tr, tb = o.insert_timed(int(u), int(v))
-            per.append(tr * (len(roots) / nr) + tb)
-        o.close()
-        per_graph.append(float(np.mean(per)))
+        r = cpu_port_time(g, roots, ins, n_ins, 0, threads)
+        per_graph.append(float(np.mean(r["t_all"])))
         total += batch * per_graph[-1]
     value = len(specs) * batch / total
     return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"every graph: min(K, {2 * threads}) roots, first {n_ins} insertions; per-root time scaled "
-                      f"to K, BC reduce added per insertion; step = {batch} insertions on each of {len(specs)} graphs",
+            "sample": f"every graph: all K roots (no extrapolation), its first {n_ins} insertions; step = {batch} "
+                      f"insertions on each of {len(specs)} graphs",
             "per_graph_insertion_ms_mean": float(np.mean(per_graph)) * 1e3}
 
 
@@ -292,29 +364,28 @@ def run_reference(args):
         print(json.dumps(line), flush=True)
         return
     need = args.warmup + args.steps
-    g, roots, ins = load_workload(args.workload, need)
-    n_roots = args.cpu_roots or min(len(roots), 2 * threads)
-    from oracle import oracle as orc
-    orc.build()
-    o = orc.PortOracle(g.nv, g.off, g.adj, roots[:n_roots], nthreads=threads)
-    o.static_timed()
-    times = []
-    for i, (u, v) in enumerate(ins[:need]):
-        tr, tb = o.insert_timed(int(u), int(v))
-        if i >= args.warmup:
-            times.append(tr * (len(roots) / n_roots) + tb)
-    o.close()
+    g, roots, ins = load_workload(args.workload, need + args.cpu_insertions_nt1)
+    r = cpu_port_time(g, roots, ins, need, args.cpu_insertions_nt1, threads)
+    times = r["t_all"][args.warmup:]
     total = float(np.sum(times))
     value = len(times) / total
+    cpu = {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"all {len(roots)} roots (no extrapolation); step i = insertion i of the stream after static "
+                     f"init ({args.warmup} untimed, {args.steps} timed), {threads} threads, timed like updateEdgeNEW "
+                     f"(per-root updates + BC reduce)"
+                     + (f"; roots in chunks of {r['chunk']} to fit host memory" if r["chunk"] < len(roots) else ""),
+           "per_insertion_ms": _lat(times), "static_init_s": r["static_s"]}
+    if args.cpu_insertions_nt1:
+        cpu["nt1"] = {"value": 1.0 / float(np.mean(r["t_one"])), "unit": UNIT, "cores": 1,
+                      "insertions": args.cpu_insertions_nt1, "per_insertion_ms": _lat(r["t_one"])}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total / len(times) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
             "impl": "reference",
             "config": {"workload": workload_desc(args.workload, g, roots), "roots": int(len(roots)),
+                       "batch": 1,
                        "step": "one insertion applied to all K roots (the reference applies insertions one at a time)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{n_roots} of {len(roots)} roots per insertion; per-root time scaled "
-                                       f"x{len(roots) / n_roots:g}, BC reduce added once"},
+            "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -344,11 +415,9 @@ def serving_set():
 
 
 def cpu_sample_serve(graphs, gid, pairs, n_ins, threads):
-    """Oracle port per graph on min(K, 2*threads) roots and its first n_ins
-    requests; the mix's CPU rate weights each graph's per-insertion time by
-    its share of the requests."""
-    from oracle import oracle as orc
-    orc.build()
+    """Oracle port per graph on all K roots and its first n_ins requests;
+    the mix's CPU rate weights each graph's per-insertion time by its share
+    of the requests."""
     share = np.bincount(gid, minlength=len(graphs)) / len(gid)
     per = []
     for i, (g, roots) in enumerate(graphs):
@@ -356,19 +425,12 @@ def cpu_sample_serve(graphs, gid, pairs, n_ins, threads):
         if not len(mine):
             per.append(0.0)
             continue
-        nr = min(len(roots), 2 * threads)
-        o = orc.PortOracle(g.nv, g.off, g.adj, roots[:nr], nthreads=threads)
-        o.static_timed()
-        ts = []
-        for u, v in mine:
-            tr, tb = o.insert_timed(int(u), int(v))
-            ts.append(tr * (len(roots) / nr) + tb)
-        o.close()
-        per.append(float(np.mean(ts)))
+        r = cpu_port_time(g, roots, mine, len(mine), 0, threads)
+        per.append(float(np.mean(r["t_all"])))
     t_mix = float(np.dot(share, per))
     return {"value": 1.0 / t_mix, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"every graph: min(K, {2 * threads}) roots, first {n_ins} of its requests; per-root time "
-                      f"scaled to K, BC reduce added; mix weighted by request share"}
+            "sample": f"every graph: all K roots (no extrapolation), first {n_ins} of its requests; mix weighted by "
+                      f"request share"}
 
 
 def run_serve(args):
@@ -544,6 +606,28 @@ def run_group(args):
         e2e = {"value": args.steps * n_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 4 * n_step,
                "d2h_bytes_per_step": 8 * nv_sum + 4 * len(specs),
                "p50_step_ms": float(np.percentile(lat, 50)), "p99_step_ms": float(np.percentile(lat, 99))}
+    # per-graph correctness, outside the timed region: every member against
+    # a static recompute (fresh graph + forest, same roots) of its graph with
+    # the insertions applied so far -- incremental must equal static exactly
+    n_applied = (args.warmup + args.steps) * B + ((1 + args.steps) * B if n_e2e else 0)
+    all_bc = grp.bc()
+    passed = 0
+    for i, ((g, roots, ins, _), (_, f)) in enumerate(zip(specs, objs)):
+        g2 = G.insert_edges(g, ins[:n_applied])
+        dg2 = native.DeviceGraph(g2.nv, g2.off, g2.adj)
+        f2 = native.DeviceForest(dg2, roots, workers=1)
+        f2.static_init()
+        d2 = f2.dist()
+        reach = d2 != np.iinfo(np.int32).max
+        ok = (np.array_equal(f.dist(), d2) and np.array_equal(f.sigma()[reach], f2.sigma()[reach]) and
+              float(np.max(np.abs(all_bc[i] - f2.bc()) / np.maximum(np.abs(f2.bc()), 1.0))) <= 1e-9)
+        passed += int(ok)
+        f2.close()
+        dg2.close()
+    check = {"graphs": len(specs), "passed": passed, "insertions_per_graph": n_applied,
+             "how": "after the timed and e2e steps: each member's dist (all vertices), sigma (reachable) and BC "
+                    "(1e-9 relative) against a static init of its updated graph on the same roots; the static "
+                    "init is pinned to the reference by the test suite"}
     cpu = None
     if not args.no_cpu and rank == 0:
         cpu = cpu_sample_group(specs, B, args.cpu_insertions // 2 or 4, os.cpu_count() or 1)
@@ -573,6 +657,7 @@ def run_group(args):
             "work": {"traversed_vertices": cnt["vertices"], "traversed_edges": cnt["edges"],
                      "scanned_slots": cnt["scanned"], "case1_pairs": cnt["case1"], "case2_pairs": cnt["case2"],
                      "insertions": args.steps * n_step},
+            "per_graph_check": check,
         }
         print(json.dumps(line), flush=True)
     grp.close()
@@ -723,16 +808,7 @@ def run_ours(args):
     upd_ms = prof["update_ms"] / upd_launches
     achieved = (alg_bytes / upd_launches) / (upd_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"k_update_{args.workload}_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            with open(tpath) as fh:
-                tj = json.load(fh)
-            if tj.get("batch") == B:
-                traffic = tj.get("bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic, traffic_note = traffic_estimate(args.workload, B, alg_bytes / upd_launches)
 
     # ---------------- plain path: one insertion per call ----------------
     plain = None
@@ -793,11 +869,10 @@ def run_ours(args):
     cpu = None
     if not args.no_cpu and rank == 0:
         threads = os.cpu_count() or 1
-        nr = args.cpu_roots or min(len(roots), 2 * threads)
-        cpu = cpu_sample(g, roots, ins_all, nr, args.cpu_insertions, threads)
+        cpu = cpu_sample(g, roots, ins_all, args.cpu_insertions, args.cpu_insertions_nt1, threads)
         if deletions:
             # a deletion on the CPU port is a recompute of every root
-            deletions["cpu_port_recompute_s_per_deletion"] = cpu["static_sample_s"] * len(roots) / nr
+            deletions["cpu_port_recompute_s_per_deletion"] = cpu["static_init_s"]
 
     info = f.info()
     if rank == 0:
@@ -818,7 +893,8 @@ def run_ours(args):
                                  "library stream; roofline: the next K batches launched directly with events "
                                  "around every kernel"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_note,
+                         "peak_source": peak_kind,
                          "kernel": "k_update", "alg_bytes_per_launch": alg_bytes / upd_launches,
                          "alg_bytes_ref_per_launch": alg_bytes_ref / upd_launches,
                          "frac_ref_equivalent": (alg_bytes_ref / upd_launches) / (upd_ms / 1e3) / 1e9 / peak,

@@ -427,22 +427,33 @@ int sbc_timer_stop(sbc_forest *f, double *ms);
  * no cudaMalloc, no cudaFree, no allocating library routine.
  *
  * All pointers are DEVICE memory owned by the caller:
- *   d_off[nv+1] int64, d_col[d_off[nv]] int32  symmetric CSR of the graph
- *   d_roots[nk] int64                          distinct root vertices
+ *   d_off[nv+1] int64, d_col[d_off[nv]] int32  symmetric CSR of the graph:
+ *                                              d_off[0] == 0, non-decreasing,
+ *                                              every neighbour id in [0, nv)
+ *   d_roots[nk] int64                          distinct root vertices, each in [0, nv)
  *   d_dist[nk][nv] int32 (INT32_MAX = unreachable), d_sigma[nk][nv] int64,
  *   d_delta[nk][nv] fp64, d_bc[nv] fp64         outputs, as sbc_get_dist/...
  * Limits: nv <= SBC_NOALLOC_MAX_VERTICES and nk * nv <= SBC_NOALLOC_MAX_CELLS;
  * larger sizes are rejected with SBC_ERR_ARG before any GPU work.
  * The work is queued on `stream` (a cudaStream_t; NULL = the legacy default
- * stream) and the call returns without waiting.
+ * stream) and the call waits for it before returning.  The ids are checked on
+ * the device first: a root or neighbour id outside [0, nv), or an offset
+ * array that does not start at 0 or decreases, makes the call return
+ * SBC_ERR_ARG without running the init (the outputs are then not written; a
+ * root outside the graph is never used as an index).
  *
  * The first call on a device looks up the device address of the array on the
- * current device (cudaGetSymbolAddress); make that first call before any CUDA
- * stream capture.  Every call on a device uses the same array and leaves its
- * contents behind for the next; what must start at zero is cleared on the
- * stream at the start of each call.  Calls whose GPU work overlaps -- on
- * different streams, or from different host threads -- race on the array and
- * give undefined results: serialise them.
+ * current device (cudaGetSymbolAddress) and keeps it for later calls on that
+ * device; make that first call before any CUDA stream capture.  The kept
+ * address belongs to the device's context at the time: after
+ * cudaDeviceReset on that device the library must be unloaded and loaded
+ * again before this entry point is used there.  Every call on a device uses
+ * the same array and leaves its contents behind for the next; what must
+ * start at zero is cleared on the stream at the start of each call.  Calls
+ * whose GPU work overlaps -- on different streams, or from different host
+ * threads -- race on the array and give undefined results: serialise them.
+ * A CUDA error left pending by earlier work of the caller is reported as
+ * such (SBC_ERR_CUDA) before anything is queued.
  * Errors: SBC_ERR_ARG, SBC_ERR_NOGPU, SBC_ERR_CUDA; message from
  * sbc_noalloc_last_error(). */
 #define SBC_NOALLOC_MAX_VERTICES 262144

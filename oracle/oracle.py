@@ -22,11 +22,27 @@ _i64p = C.POINTER(C.c_int64)
 _f64p = C.POINTER(C.c_double)
 
 
+def reference_src() -> str:
+    """Directory of the reference's C sources: $SBC_REFERENCE_SRC when set,
+    else the Makefile's overridable REF default."""
+    env = os.environ.get("SBC_REFERENCE_SRC")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+def reference_available() -> bool:
+    src = reference_src()
+    return bool(src) and os.path.isfile(os.path.join(src, "streamingbc.c"))
+
+
 def build(ref: bool = False) -> None:
-    """Compile liboracle.so (and the reference harness when ``ref``)."""
+    """Compile liboracle.so (and the reference harness when ``ref``, from
+    reference_src())."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={reference_src()}"], check=True)
 
 
 def _p64(a: np.ndarray):
@@ -67,6 +83,7 @@ def _port_lib():
         lib.orc_insert_timed.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, _f64p, _f64p]
         lib.orc_static_timed.restype = C.c_double
         lib.orc_static_timed.argtypes = [C.c_void_p, C.c_void_p]
+        lib.orc_set_threads.argtypes = [C.c_void_p, C.c_int64]
         _port = lib
     return _port
 
@@ -107,6 +124,10 @@ class PortOracle:
 
     def static(self):
         self.lib.orc_static(self.f, self.g)
+
+    def set_threads(self, n: int) -> None:
+        """Threads of the following calls (1 .. nthreads): the reference's NT."""
+        self.lib.orc_set_threads(self.f, int(n))
 
     def insert(self, u: int, v: int) -> None:
         """Insert (u,v) into the graph (both directions), then update every root."""

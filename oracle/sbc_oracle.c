@@ -138,6 +138,7 @@ typedef struct {
 
 typedef struct {
     int64_t nv, nk, nt;
+    int64_t nt_active; /* threads the parallel loops use (<= nt; the reference's NT) */
     int64_t *roots;
     int64_t *level;   /* [nk][nv] */
     int64_t *sigma;   /* [nk][nv] */
@@ -184,7 +185,7 @@ orc_forest *orc_forest_new(int64_t nv, int64_t nk, const int64_t *roots, int64_t
     if (nt < 1) nt = 1;
     orc_forest *f = (orc_forest *)calloc(1, sizeof(orc_forest));
     if (!f) return NULL;
-    f->nv = nv; f->nk = nk; f->nt = nt;
+    f->nv = nv; f->nk = nk; f->nt = nt; f->nt_active = nt;
     f->roots = (int64_t *)malloc((size_t)nk * sizeof(int64_t));
     memcpy(f->roots, roots, (size_t)nk * sizeof(int64_t));
     size_t cells = (size_t)nk * (size_t)nv;
@@ -206,6 +207,14 @@ void orc_forest_free(orc_forest *f)
     free(f);
 }
 
+/* Threads used by the following calls (1 .. the count the forest was made
+ * with): the reference's NT, which its COARSE loop hands to
+ * omp_set_num_threads (src/streamingbc.c:168). */
+void orc_set_threads(orc_forest *f, int64_t nt)
+{
+    f->nt_active = nt < 1 ? 1 : (nt > f->nt ? f->nt : nt);
+}
+
 int64_t *orc_forest_level(orc_forest *f) { return f->level; }
 int64_t *orc_forest_sigma(orc_forest *f) { return f->sigma; }
 double *orc_forest_delta(orc_forest *f) { return f->delta; }
@@ -220,7 +229,9 @@ void orc_forest_counters(const orc_forest *f, int64_t *out4)
  * src/streamingbc.c:211-218 and src/streamingbc_init.c:76-83. */
 static void reduce_bc(orc_forest *f)
 {
-    int64_t nv = f->nv, nt = f->nt;
+    /* only the active threads' partials can be nonzero: every call clears
+     * the partials it folds, so a later call with fewer threads sees zeros */
+    int64_t nv = f->nv, nt = f->nt_active;
     #pragma omp parallel for num_threads(nt)
     for (int64_t v = 0; v < nv; v++) {
         for (int64_t t = 0; t < nt; t++) {
@@ -289,7 +300,7 @@ static void static_root(const orc_graph *g, orc_forest *f, int64_t r, orc_scratc
 void orc_static(orc_forest *f, const orc_graph *g)
 {
     for (int64_t v = 0; v < f->nv; v++) f->bc[v] = 0.0;
-    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt)
+    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt_active)
     for (int64_t r = 0; r < f->nk; r++)
         static_root(g, f, r, &f->scr[omp_get_thread_num()]);
     reduce_bc(f);
@@ -559,7 +570,7 @@ static void insert_root(const orc_graph *g, orc_forest *f, int64_t r,
 
 void orc_insert(orc_forest *f, const orc_graph *g, int64_t u, int64_t v)
 {
-    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt)
+    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt_active)
     for (int64_t r = 0; r < f->nk; r++)
         insert_root(g, f, r, u, v, &f->scr[omp_get_thread_num()]);
     reduce_bc(f);
@@ -571,7 +582,7 @@ void orc_insert(orc_forest *f, const orc_graph *g, int64_t u, int64_t v)
 void orc_insert_timed(orc_forest *f, const orc_graph *g, int64_t u, int64_t v, double *t_roots, double *t_reduce)
 {
     double t0 = omp_get_wtime();
-    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt)
+    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt_active)
     for (int64_t r = 0; r < f->nk; r++)
         insert_root(g, f, r, u, v, &f->scr[omp_get_thread_num()]);
     double t1 = omp_get_wtime();
@@ -586,7 +597,7 @@ double orc_static_timed(orc_forest *f, const orc_graph *g)
 {
     double t0 = omp_get_wtime();
     for (int64_t x = 0; x < f->nv; x++) f->bc[x] = 0.0;
-    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt)
+    #pragma omp parallel for schedule(dynamic, 1) num_threads(f->nt_active)
     for (int64_t r = 0; r < f->nk; r++)
         static_root(g, f, r, &f->scr[omp_get_thread_num()]);
     reduce_bc(f);

@@ -2177,23 +2177,46 @@ StreamingExtraInfo deleteEdgeStreamingBC(bcForest* forest, struct stinger* sStin
     return sei;
 }
 
-// src/streamingbc.c:56-77: insert every edge of the new vertex, one at a time.
+// src/streamingbc.c:56-77: the reference inserts the vertex's edges (src,
+// adjacencyArray[d]) into the graph and updates the forest one edge at a
+// time.  Here all of them go to the device as one batch (sbc_insert_batch):
+// appended in array order, each applied to every root in that order, so the
+// state is the one the edge-by-edge loop reaches, in one append, one
+// classify and one update launch instead of one synchronous call per edge.
+// An entry that is already an edge, repeats an earlier entry, is src itself
+// or lies outside the graph is skipped (the reference would apply the update
+// of an existing edge a second time).
 StreamingExtraInfo insertVertexStreamingBC(bcForest* forest, struct stinger* sStinger, int64_t src,
                                            int64_t* adjacencyArray, int64_t adjacencySize,
                                            int64_t* rootArrayForApproximation, int64_t NK, int64_t NV, int64_t NT,
                                            extraArraysPerThread** eAPT)
 {
+    (void)rootArrayForApproximation;
+    (void)NV;
+    (void)NT;
     StreamingExtraInfo total = {0, 0, 0, 0};
-    for (int64_t d = 0; d < adjacencySize; ++d) {
-        const int64_t dest = adjacencyArray[d];
-        stinger_insert_edge(sStinger, 0, src, dest, 0, 0);
-        stinger_insert_edge(sStinger, 0, dest, src, 0, 0);
-        StreamingExtraInfo one = insertEdgeStreamingBC(forest, sStinger, src, dest, rootArrayForApproximation, NK, NV,
-                                                       NT, eAPT, BALANCE, FINE);
-        total.adjacent += one.adjacent;
-        total.movement += one.movement;
-        total.sameLevel += one.sameLevel;
+    if (!forest || !forest->sbc || !sStinger || forest->sbc->g != sStinger->g) {
+        fail(SBC_ERR_STATE, "insertVertexStreamingBC: static init on this graph has not run");
+        return total;
     }
+    if (adjacencySize <= 0) return total;
+    if (!adjacencyArray) {
+        fail(SBC_ERR_ARG, "insertVertexStreamingBC: null adjacency array");
+        return total;
+    }
+    std::vector<int64_t> us((size_t)adjacencySize, src);
+    sbc_batch_stats st;
+    if (sbc_insert_batch(forest->sbc, adjacencySize, us.data(), adjacencyArray, &st)) return total;
+    total.adjacent = st.case1;
+    total.movement = st.case2;
+    total.sameLevel = NK * st.inserted - st.case1 - st.case2;
+    if (eAPT && eAPT[0]) {
+        eAPT[0]->adjacentCounter += st.case1;
+        eAPT[0]->movementCounter += st.case2;
+        eAPT[0]->dynamicTraverseVerticeCounter += st.vertices;
+        eAPT[0]->dynamicTraverseEdgeCounter += st.edges;
+    }
+    refresh_bc(forest);
     return total;
 }
 

@@ -35,6 +35,7 @@ struct StaticArgs {
     unsigned long long* counters;  // [0] vertices, [1] edges
     const int* list;   // roots to (re)compute, or null for all
     const int* nlist;
+    const int* abort;  // when non-null and set, the launch does nothing (inputs failed a device check)
 };
 
 template <int NT>
@@ -46,6 +47,7 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
     __shared__ double s_acc[NT];
     __shared__ int s_hit[NT];
     const int64_t nv = A.nv;
+    if (A.abort && *A.abort) return;
     Scratch W = A.scr.of(blockIdx.x, nv);
     if (threadIdx.x == 0) sm.walked_v = sm.walked_e = sm.scanned_e = 0;
 
@@ -60,7 +62,8 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         uint8_t* D8 = A.dist8 + (size_t)r * nv;
         int64_t* Sg = A.sigma + (size_t)r * nv;
         double* Dl = A.delta + (size_t)r * nv;
-        const int root = (int)A.roots[r];
+        const int64_t root64 = A.roots[r];
+        const int root = (int)root64;
 
         for (int64_t x = threadIdx.x; x < nv; x += NT) {
             D[x] = SBC_INF;
@@ -69,6 +72,9 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
             Dl[x] = 0.0;
         }
         __syncthreads();
+        // a root outside the graph (only possible through callers whose roots
+        // are not checked on the host) keeps an empty tree
+        if (root64 < 0 || root64 >= nv) continue;
         if (threadIdx.x == 0) {
             D[root] = 0;
             D8[root] = 0;
@@ -190,6 +196,7 @@ cudaError_t launch_static_list(sbc_forest* f, const int* d_list, const int* d_nl
     A.counters = f->d_counters;
     A.list = d_list;
     A.nlist = d_nlist;
+    A.abort = nullptr;
     // One worker slot per CTA: with few workers per SM, wider CTAs keep the SMs full.
     const int grid = (int)std::min<int64_t>(f->workers, f->nk);
     const int64_t per_sm = (f->workers + f->sm_count - 1) / f->sm_count;
@@ -251,12 +258,61 @@ __global__ void k_csr_degrees(const int64_t* __restrict__ off, int64_t nv, int32
         deg[v] = (int32_t)(off[v + 1] - off[v]);
 }
 
+// Input check on the device, before k_static touches anything: a root outside
+// [0, nv), an offset array that does not start at 0 or decreases, or a
+// neighbour id outside [0, nv) sets a bit of *bad (1 roots, 2 offsets, 4
+// neighbour ids).  k_static and k_bc_colsum_checked read the word and do
+// nothing when it is set, so a bad id never becomes an out-of-bounds access.
+// The neighbour ids read are d_col[0 .. d_off[nv]), the caller's CSR.
+__global__ void k_noalloc_check(const int64_t* __restrict__ off, const int32_t* __restrict__ col, int64_t nv,
+                                const int64_t* __restrict__ roots, int64_t nk, int* __restrict__ bad)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int flags = 0;
+    for (int64_t r = t0; r < nk; r += stride)
+        if (roots[r] < 0 || roots[r] >= nv) flags |= 1;
+    for (int64_t v = t0; v < nv; v += stride)
+        if (off[v + 1] < off[v] || (v == 0 && off[0] != 0)) flags |= 2;
+    const int64_t ne = off[nv];
+    for (int64_t i = t0; i < ne; i += stride) {
+        const int32_t c = col[i];
+        if (c < 0 || (int64_t)c >= nv) flags |= 4;
+    }
+    if (flags) atomicOr(bad, flags);
+}
+
+__global__ void k_bc_colsum_checked(const double* __restrict__ delta, const int64_t* __restrict__ roots, int nk,
+                                    int64_t nv, double* __restrict__ bc, const int* __restrict__ bad)
+{
+    if (*bad) return;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int r = 0; r < nk; ++r) {
+            const double d = delta[(size_t)r * nv + v];
+            if (roots[r] != v) s += d;
+        }
+        bc[v] = s;
+    }
+}
+
 thread_local std::string t_noalloc_err;
 
-int noalloc_fail(int code, const char* msg)
+int noalloc_fail(int code, const std::string& msg)
 {
     t_noalloc_err = msg;
     return code;
+}
+
+// Status of the launch just queued: a launch error names the kernel.
+bool noalloc_launch_failed(const char* kernel, int* rc)
+{
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) return false;
+    *rc = noalloc_fail(SBC_ERR_CUDA, std::string("sbc_static_init_noalloc: ") + kernel + " launch failed: " +
+                                         cudaGetErrorString(e));
+    return true;
 }
 
 }  // namespace
@@ -277,6 +333,12 @@ extern "C" int sbc_static_init_noalloc(int64_t nv, const int64_t* d_off, const i
     if (nk > nv || nk * nv > kNoallocMaxCells)
         return noalloc_fail(SBC_ERR_ARG,
                             "sbc_static_init_noalloc: roots x vertices exceeds SBC_NOALLOC_MAX_CELLS (or nk > nv)");
+    // an error left by earlier work of the caller is reported as such, not
+    // as a failure of this call's launches
+    const cudaError_t pending = cudaGetLastError();
+    if (pending != cudaSuccess)
+        return noalloc_fail(SBC_ERR_CUDA, std::string("sbc_static_init_noalloc: CUDA error pending from earlier "
+                                                      "work before the call: ") + cudaGetErrorString(pending));
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256)
         return noalloc_fail(SBC_ERR_NOGPU, "sbc_static_init_noalloc: no current CUDA device");
@@ -285,24 +347,31 @@ extern "C" int sbc_static_init_noalloc(int64_t nv, const int64_t* d_off, const i
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
         if (!g_noalloc_ptr[dev]) {
             void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
-                return noalloc_fail(SBC_ERR_CUDA, "sbc_static_init_noalloc: cudaGetSymbolAddress failed");
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p)
+                return noalloc_fail(SBC_ERR_CUDA, std::string("sbc_static_init_noalloc: cudaGetSymbolAddress "
+                                                              "failed: ") + cudaGetErrorString(e));
             g_noalloc_ptr[dev] = p;
         }
         base = (unsigned char*)g_noalloc_ptr[dev];
     }
     cudaStream_t s = (cudaStream_t)stream;
     unsigned long long* counters = (unsigned long long*)(base + kOffCounters);
+    int* bad = (int*)(counters + 12);
     int32_t* deg = (int32_t*)(base + kOffDeg);
     const int slots = (int)std::min<int64_t>(kNoallocSlots, nk);
-    // Clear what must start at zero: the work and traversal counters and the
-    // accumulators (a previous call leaves them zero, but a call that failed
-    // half-way may not have).
+    // Clear what must start at zero: the work and traversal counters, the
+    // input-check word and the accumulators (a previous call leaves them
+    // zero, but a call that failed half-way may not have).
     if (cudaMemsetAsync(counters, 0, 16 * sizeof(unsigned long long), s) != cudaSuccess ||
         cudaMemsetAsync(base + kOffAcc, 0, sizeof(double) * (size_t)slots * (size_t)nv, s) != cudaSuccess)
         return noalloc_fail(SBC_ERR_CUDA, "sbc_static_init_noalloc: clearing scratch failed");
     const int dgrid = (int)std::min<int64_t>((nv + 255) / 256, 4096);
+    int rc = SBC_OK;
+    k_noalloc_check<<<dgrid, 256, 0, s>>>(d_off, d_col, nv, d_roots, nk, bad);
+    if (noalloc_launch_failed("k_noalloc_check", &rc)) return rc;
     k_csr_degrees<<<dgrid, 256, 0, s>>>(d_off, nv, deg);
+    if (noalloc_launch_failed("k_csr_degrees", &rc)) return rc;
 
     StaticArgs A;
     A.G.nv = nv;
@@ -333,8 +402,24 @@ extern "C" int sbc_static_init_noalloc(int64_t nv, const int64_t* d_off, const i
     A.counters = counters;
     A.list = nullptr;
     A.nlist = nullptr;
+    A.abort = bad;
     k_static<1024><<<slots, 1024, 0, s>>>(A);
-    k_bc_colsum<<<dgrid, 256, 0, s>>>(d_delta, d_roots, (int)nk, nv, d_bc);
-    if (cudaGetLastError() != cudaSuccess) return noalloc_fail(SBC_ERR_CUDA, "sbc_static_init_noalloc: launch failed");
+    if (noalloc_launch_failed("k_static", &rc)) return rc;
+    k_bc_colsum_checked<<<dgrid, 256, 0, s>>>(d_delta, d_roots, (int)nk, nv, d_bc, bad);
+    if (noalloc_launch_failed("k_bc_colsum", &rc)) return rc;
+    // wait for the work and read the input-check word (a 4-byte copy into a
+    // stack variable: no allocation)
+    int h_bad = 0;
+    cudaError_t e = cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return noalloc_fail(SBC_ERR_CUDA, std::string("sbc_static_init_noalloc: ") + cudaGetErrorString(e));
+    if (h_bad) {
+        std::string m = "sbc_static_init_noalloc: inputs rejected on the device (outputs not written):";
+        if (h_bad & 1) m += " a root outside [0, nv);";
+        if (h_bad & 2) m += " d_off not a CSR offset array (d_off[0] != 0 or decreasing);";
+        if (h_bad & 4) m += " a neighbour id outside [0, nv);";
+        return noalloc_fail(SBC_ERR_ARG, m);
+    }
     return SBC_OK;
 }

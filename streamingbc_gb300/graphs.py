@@ -331,15 +331,16 @@ def rmat_group(count: int = 64, scale_lo: int = 10, scale_hi: int = 16, edge_fac
 
 
 def serving_graphs(count: int = 16, n_lo: float = 1e4, n_hi: float = 1e6, gamma: float = 2.3,
-                   avg_degree: float = 12.0, seed0: int = 200, k: int = 512):
+                   avg_degree: float = 12.0, seed0: int = 200, k: int = 512, only=None):
     """Graphs for the serving loop: Chung-Lu graph i has n_i = n_lo *
     (n_hi/n_lo)^(i/(count-1)) vertices (log-spaced), m = avg_degree * n_i / 2
     expected edges, power-law exponent gamma, expected degrees in
     [1, sqrt(2m)] (the structural cutoff), seed seed0 + i; the largest
     connected component is kept.  K = min(|V|, k) uniform roots each.
+    `only` (an iterable of indices) builds just those members of the set.
     Returns a list of (graph, roots)."""
     out = []
-    for i in range(count):
+    for i in (range(count) if only is None else only):
         n = int(round(n_lo * (n_hi / n_lo) ** (i / max(count - 1, 1))))
         m = int(round(avg_degree * n / 2))
         g = chung_lu(n, m, gamma, 1.0, float(np.sqrt(2.0 * m)), seed=seed0 + i)

@@ -4,7 +4,8 @@
  * :458-471): CSR -> CreateStingerFromCSR -> forest + auxiliary arrays -> static
  * init -> for each insertion: stinger_insert_edge x2, insertEdgeStreamingBC;
  * then for each deletion: stinger_remove_edge x2, deleteEdgeStreamingBC;
- * then optionally deleteVertexStreamingBC of one vertex.
+ * then optionally deleteVertexStreamingBC of one vertex, then optionally
+ * insertVertexStreamingBC of one vertex with a list of neighbours.
  * Compiled with plain gcc against include/streamingbc.h and linked to
  * libsbc_gb300.so; nothing in it knows about CUDA.
  *
@@ -117,6 +118,42 @@ int main(int argc, char **argv)
         fprintf(out, "vbc 0");
         for (long long x = 0; x < NV; x++) fprintf(out, " %.17g", forest->totalBC[x]);
         fprintf(out, "\n");
+        free(adj);
+    }
+
+    /* optional: insert a vertex's edges (insertVertexStreamingBC inserts them
+     * into the graph itself, src/streamingbc.c:56-77) */
+    long long VI = -1, NVI = 0;
+    if (fscanf(in, "%lld %lld", &VI, &NVI) != 2) VI = -1;
+    if (VI >= 0) {
+        int64_t *adj = (int64_t *)malloc(sizeof(int64_t) * (size_t)(NVI > 0 ? NVI : 1));
+        for (long long i = 0; i < NVI; i++) {
+            long long x;
+            if (fscanf(in, "%lld", &x) != 1) return 3;
+            adj[i] = x;
+        }
+        StreamingExtraInfo sei = insertVertexStreamingBC(forest, G, VI, adj, NVI, roots, NK, NV, NT, aux);
+        if (sbc_last_error()[0]) {
+            fprintf(stderr, "insert vertex: %s\n", sbc_last_error());
+            return 9;
+        }
+        fprintf(out, "ivdeg %lld %lld %lld\n", (long long)stinger_outdegree(G, VI), (long long)sei.adjacent,
+                (long long)sei.movement);
+        fprintf(out, "ivbc 0");
+        for (long long x = 0; x < NV; x++) fprintf(out, " %.17g", forest->totalBC[x]);
+        fprintf(out, "\n");
+        if (streamingBCSyncForest(forest) != 0) {
+            fprintf(stderr, "sync: %s\n", sbc_last_error());
+            return 5;
+        }
+        for (long long r = 0; r < NK; r++) {
+            bcTree *t = forest->forest[roots[r]];
+            fprintf(out, "ivlv %lld", r);
+            for (long long x = 0; x < NV; x++) fprintf(out, " %lld", (long long)t->vArr[x].level);
+            fprintf(out, "\nivsg %lld", r);
+            for (long long x = 0; x < NV; x++) fprintf(out, " %lld", (long long)t->vArr[x].sigma);
+            fprintf(out, "\n");
+        }
         free(adj);
     }
     streamingBCDeleteAuxilary(aux, NT, NV);

@@ -54,11 +54,19 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case, port
         for u, v in dels:
             fh.write(f"{u} {v}\n")
         fh.write("1\n")  # then delete vertex 1 with all its edges
+        # then re-insert vertex 1 with every other former neighbour, a vertex
+        # it never had as a neighbour, a repeated entry and a self-loop (the
+        # last two are skipped)
+        src0 = list(dict.fromkeys([int(y) for y in z["adj"][z["off"][1]:z["off"][2]]]))
+        back = src0[::2]
+        far = next(y for y in range(nv - 1, -1, -1) if y != 1 and y not in src0)
+        vins = back + [far, back[0], 1]
+        fh.write(f"1 {len(vins)} " + " ".join(map(str, vins)) + "\n")
     outp = tmp_path / "out.txt"
     r = subprocess.run([str(driver), str(inp), str(outp)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     bc, lv, sg = {}, {}, {}
-    deg0 = vdeg = None
+    deg0 = vdeg = ivdeg = None
     for line in open(outp):
         p = line.split()
         if p[0] == "bc":
@@ -75,6 +83,14 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case, port
             bc["vertex"] = np.array(p[2:], dtype=np.float64)
         elif p[0] == "vdeg":
             vdeg = (int(p[1]), int(p[2]))
+        elif p[0] == "ivbc":
+            bc["ivertex"] = np.array(p[2:], dtype=np.float64)
+        elif p[0] == "ivlv":
+            lv[("iv", int(p[1]))] = np.array(p[2:], dtype=np.int64)
+        elif p[0] == "ivsg":
+            sg[("iv", int(p[1]))] = np.array(p[2:], dtype=np.int64)
+        elif p[0] == "ivdeg":
+            ivdeg = int(p[1])
     assert bc_err(bc[-1], z["bc0"]) <= BC_RTOL
     for i in range(len(z["ins"])):
         assert bc_err(bc[i], z["bc_trace"][i]) <= BC_RTOL, f"bc after insertion {i}"
@@ -99,6 +115,14 @@ def test_reference_style_c_caller_matches_reference(driver, tmp_path, case, port
         o.delete(1, y)
     assert vdeg == (len(nb), 0)
     assert bc_err(bc["vertex"], o.bc()) <= BC_RTOL
+    # vertex 1 re-inserted: its new edges one at a time in the oracle
+    new = list(dict.fromkeys(y for y in back + [far] if y != 1))
+    for y in new:
+        o.insert(1, y)
+    assert ivdeg == len(new)
+    assert bc_err(bc["ivertex"], o.bc()) <= BC_RTOL
+    assert_levels(np.stack([lv[("iv", r)] for r in range(k)]), o.level())
+    assert_sigma(np.stack([sg[("iv", r)] for r in range(k)]), o.sigma(), o.level())
     o.close()
 
 

@@ -37,12 +37,19 @@ def _entry(lib):
     return fn
 
 
-def _run_noalloc(lib, g, roots):
+def _run_noalloc(lib, g, roots, stream=None, adj=None):
+    """Outputs of one call (rc 0 asserted); `stream` a torch.cuda.Stream or None."""
+    rc, out = _call_noalloc(lib, g, roots, stream=stream, adj=adj)
+    assert rc == 0, lib.sbc_noalloc_last_error().decode()
+    return out
+
+
+def _call_noalloc(lib, g, roots, stream=None, adj=None):
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda")
     k, n = len(roots), g.nv
     off = torch.tensor(g.off, dtype=torch.int64, device=dev)
-    col = torch.tensor(g.adj, dtype=torch.int32, device=dev)
+    col = torch.tensor(g.adj if adj is None else adj, dtype=torch.int32, device=dev)
     rt = torch.tensor(roots, dtype=torch.int64, device=dev)
     # outputs start as garbage: every entry must be written by the call
     dist = torch.full((k, n), -7, dtype=torch.int32, device=dev)
@@ -50,11 +57,11 @@ def _run_noalloc(lib, g, roots):
     delta = torch.full((k, n), float("nan"), dtype=torch.float64, device=dev)
     bc = torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
+    handle = None if stream is None else stream.cuda_stream
     rc = _entry(lib)(n, off.data_ptr(), col.data_ptr(), k, rt.data_ptr(), dist.data_ptr(), sigma.data_ptr(),
-                     delta.data_ptr(), bc.data_ptr(), None)
-    assert rc == 0, lib.sbc_noalloc_last_error().decode()
+                     delta.data_ptr(), bc.data_ptr(), handle)
     torch.cuda.synchronize()
-    return dist.cpu().numpy(), sigma.cpu().numpy(), delta.cpu().numpy(), bc.cpu().numpy()
+    return rc, (dist.cpu().numpy(), sigma.cpu().numpy(), delta.cpu().numpy(), bc.cpu().numpy())
 
 
 def _run_existing(g, roots):
@@ -96,3 +103,35 @@ def test_noalloc_rejects_sizes_beyond_its_maximum(sbc_lib):
     rc = fn(100000, p, p, 100, p, p, p, p, p, None)  # 1e7 cells > SBC_NOALLOC_MAX_CELLS
     assert rc == -1
     assert b"SBC_NOALLOC_MAX_CELLS" in sbc_lib.sbc_noalloc_last_error()
+
+
+def test_noalloc_on_a_caller_stream_with_fewer_roots_than_worker_slots(sbc_lib):
+    """Work queued on a stream the caller created, and nk (3) below the
+    array's worker slots, so fewer CTAs run than slots exist."""
+    torch = pytest.importorskip("torch")
+    g = G.er(500, 2000, seed=43)
+    r = G.pick_roots(g.nv, 3, seed=43)
+    st = torch.cuda.Stream()
+    _check(_run_noalloc(sbc_lib, g, r, stream=st), _run_existing(g, r))
+    _check(_run_noalloc(sbc_lib, g, r, stream=st), _run_existing(g, r))
+
+
+def test_noalloc_rejects_ids_outside_the_graph(sbc_lib):
+    """A root or a neighbour id outside [0, nv) is caught on the device
+    before the init runs: the call returns SBC_ERR_ARG and writes nothing,
+    and the next valid call is unaffected."""
+    g = G.er(400, 1600, seed=44)
+    r = G.pick_roots(g.nv, 6, seed=44)
+    bad_roots = np.array(r, dtype=np.int64)
+    bad_roots[2] = g.nv + 5
+    rc, (d, s, dl, bc) = _call_noalloc(sbc_lib, g, bad_roots)
+    assert rc == -1
+    assert b"root outside" in sbc_lib.sbc_noalloc_last_error()
+    assert (d == -7).all() and (s == -7).all() and np.isnan(bc).all()
+    bad_adj = np.array(g.adj, dtype=np.int32)
+    bad_adj[len(bad_adj) // 2] = g.nv
+    rc, (d, s, dl, bc) = _call_noalloc(sbc_lib, g, r, adj=bad_adj)
+    assert rc == -1
+    assert b"neighbour id outside" in sbc_lib.sbc_noalloc_last_error()
+    assert (d == -7).all() and np.isnan(bc).all()
+    _check(_run_noalloc(sbc_lib, g, r), _run_existing(g, r))
