@@ -52,7 +52,11 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", choices=["rmat20", "rmat18", "rmat16", "chunglu40k", "er1024", "rmat_group64",
-                                          "serve16"], default="rmat20")
+                                          "serve16", "serve_rmat20"], default="rmat20")
+    p.add_argument("--served-rate", type=float, default=4000.0,
+                   help="rmat20 served form: offered insertions/s (Poisson)")
+    p.add_argument("--served-requests", type=int, default=16384, help="rmat20 served form: timed requests")
+    p.add_argument("--no-served", action="store_true", help="rmat20: skip the served form")
     p.add_argument("--serve-rate", type=float, default=50000.0, help="serve16: offered insertions/s")
     p.add_argument("--serve-requests", type=int, default=10000, help="serve16: timed requests")
     p.add_argument("--serve-max-batch", type=int, default=1024)
@@ -527,6 +531,59 @@ def run_serve(args):
         print(json.dumps(line), flush=True)
 
 
+def serve_one(g, roots, reqs, rate, n_warm, n_req, n_plain, max_batch, train, budget, local):
+    """One graph through the serving loop: requests arrive as a Poisson
+    process of `rate`/s.  Batched form: launch shape tuned on the first batch,
+    cost model trained on the costs of the first `train` insertions, then the
+    model's schedule; the first n_warm requests (tuning, logging, training)
+    are untimed, the next n_req timed.  Plain form: a fresh server applying
+    one request at a time (max_batch 1, one batch in flight), n_plain
+    requests offered at the same rate."""
+    from streamingbc_gb300 import native
+    rng = np.random.default_rng(23)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n_warm + n_req + n_plain))
+    gid = np.zeros(len(t), dtype=np.int32)
+
+    def run(mb, lo, warm_hi, hi, inflight, tune, tr):
+        srv = native.DeviceServer(budget_bytes=budget, max_batch=mb, max_inflight=inflight, autotune=tune,
+                                  train_insertions=tr)
+        srv.add_graph(g, roots)
+        srv.drain()
+        if warm_hi > lo:
+            srv.play(gid[lo:warm_hi], reqs[lo:warm_hi], t[lo:warm_hi] - t[lo])
+            srv.drain()
+            srv.stats(reset=True)
+        clk = ClockSampler(local)
+        clk.start()
+        t1 = time.perf_counter()
+        srv.play(gid[warm_hi:hi], reqs[warm_hi:hi], t[warm_hi:hi] - t[warm_hi])
+        srv.drain()
+        wall = time.perf_counter() - t1
+        clocks = clk.stop()
+        st = srv.stats()
+        srv.close()
+        return st, wall, clocks
+
+    st, wall, clocks = run(max_batch, 0, n_warm, n_warm + n_req, 0, True, train)
+    out = {"value": st["throughput"], "unit": UNIT, "offered_rate": rate, "requests": n_req,
+           "latency_ms": {"p50": st["p50_us"] / 1e3, "p99": st["p99_us"] / 1e3, "mean": st["mean_us"] / 1e3,
+                          "max": st["max_us"] / 1e3},
+           "mean_batch": st["mean_batch"], "batches": st["batches"], "wall_s": wall, "clocks": clocks,
+           "how": f"sbc_server, one resident graph; first {n_warm} requests untimed (launch shape tuned on the first "
+                  f"batch, per-job costs of {train} insertions logged, cost model trained, model schedule after); "
+                  f"throughput = completed / (last completion - first arrival); latency = arrival to batch "
+                  f"completion"}
+    if n_plain:
+        lo = n_warm + n_req
+        pst, pwall, _ = run(1, lo, lo, lo + n_plain, 1, True, 0)
+        out["plain"] = {"value": pst["throughput"], "unit": UNIT, "requests": n_plain,
+                        "latency_ms": {"p50": pst["p50_us"] / 1e3, "p99": pst["p99_us"] / 1e3},
+                        "how": "same server and arrival process, one request per batch and one batch in flight: the "
+                               "unbatched plain GPU path (overloaded at this rate: latency is queueing)"}
+        out["served_over_plain"] = out["value"] / pst["throughput"] if pst["throughput"] else None
+    return out
+
+
 def run_group(args):
     """64 R-MAT graphs updated together: one group batch (append, classify,
     update, seal over all graphs) per step."""
@@ -691,7 +748,8 @@ def run_ours(args):
     n_cmp = args.compare_batches * B if train > 0 else 0
     n_pre = train + n_cmp
     t0 = time.time()
-    g, roots, ins_all = load_workload(args.workload, n_pre + n_dev + n_e2e + n_plain)
+    n_served = 0 if (args.workload != "rmat20" or args.no_served) else 16384 + 2 * B + args.served_requests + 2048
+    g, roots, ins_all = load_workload(args.workload, max(n_pre + n_dev + n_e2e + n_plain, n_served))
     if args.roots:
         roots = roots[:args.roots]
     if world > 1:
@@ -875,6 +933,12 @@ def run_ours(args):
             deletions["cpu_port_recompute_s_per_deletion"] = cpu["static_init_s"]
 
     info = f.info()
+    served = None
+    if args.workload == "rmat20" and not args.no_served and world == 1:
+        f.close()
+        dg.close()
+        served = serve_one(g, roots, ins_all[:n_served], args.served_rate, 16384 + 2 * B, args.served_requests,
+                           2048, args.serve_max_batch, 16384, int(args.serve_budget_gb * (1 << 30)), local)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -914,10 +978,12 @@ def run_ours(args):
                      "scanned_slots": cnt["scanned"], "case1_pairs": cnt["case1"], "case2_pairs": cnt["case2"],
                      "insertions": n_timed},
             "kernel_ms": {k: prof[k] for k in ("append_ms", "classify_ms", "update_ms", "batch_ms")},
+            "served": served,
         }
         print(json.dumps(line), flush=True)
-    f.close()
-    dg.close()
+    if served is None:
+        f.close()
+        dg.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -303,6 +303,17 @@ int sbc_server_destroy(sbc_server *s);
  * default, means no limit); graphs are served round-robin.  max_batch 1 with
  * max_inflight 1 is the plain path: one insertion at a time. */
 int sbc_server_set_max_inflight(sbc_server *s, int max_inflight);
+/* Tuning of the served graphs (off by default; set before requests arrive).
+ * autotune != 0: a graph registered with variant -1 has its first batch of
+ * at least 64 requests (any size when max_batch < 64) applied through
+ * sbc_forest_autotune, which keeps the fastest launch shape for its later
+ * batches.  train_insertions > 0: every graph logs its jobs'
+ * costs over its first train_insertions applied insertions (after the tuned
+ * batch), then trains its cost model (sbc_cost_model_train: 4 epochs,
+ * minibatch 4096, lr 2e-3, 10 % held out) and is scheduled by it
+ * (SBC_SCHED_MODEL); with fewer than 128 logged jobs to train on it keeps the
+ * static schedule.  Neither changes any result. */
+int sbc_server_set_tuning(sbc_server *s, int autotune, int64_t train_insertions);
 /* Register a graph (symmetric CSR, copied) with nk roots; variant -1 picks the
  * update launch shape by size.  *id is its index (0, 1, ...). */
 int sbc_server_add_graph(sbc_server *s, int64_t nv, const int64_t *off, const int64_t *adj, int64_t nk,

@@ -402,6 +402,7 @@ struct TrialState {
     int64_t nk = 0;
     int32_t* dist = nullptr;
     uint8_t* dist8 = nullptr;
+    uint32_t* dist2 = nullptr;
     int64_t* sigma = nullptr;
     double* delta = nullptr;
     double* bc = nullptr;
@@ -412,7 +413,8 @@ struct TrialState {
         nk = rows;
         const size_t cells = (size_t)rows * (size_t)f->nv;
         cudaError_t e;
-        if ((e = dev_alloc(&dist, cells)) || (e = dev_alloc(&dist8, cells)) || (e = dev_alloc(&sigma, cells)) ||
+        if ((e = dev_alloc(&dist, cells)) || (e = dev_alloc(&dist8, cells)) ||
+            (e = dev_alloc(&dist2, (size_t)rows * (size_t)sbc::d2_words(f->nv))) || (e = dev_alloc(&sigma, cells)) ||
             (e = dev_alloc(&delta, cells)) || (e = dev_alloc(&bc, f->nv)) ||
             (f->d_lvlhist && (e = dev_alloc(&hist, (size_t)rows * sbc::kHistLevels))) ||
             (f->d_roster && ((e = dev_alloc(&roster, (size_t)rows * sbc::kRosterLevels * sbc::kRosterCap)) ||
@@ -425,6 +427,7 @@ struct TrialState {
     {
         dev_free(dist);
         dev_free(dist8);
+        dev_free(dist2);
         dev_free(sigma);
         dev_free(delta);
         dev_free(bc);
@@ -440,6 +443,8 @@ struct TrialState {
         cudaError_t e;
         if ((e = cudaMemcpyAsync(dist, f->d_dist, sizeof(int32_t) * cells, d2d, s)) ||
             (e = cudaMemcpyAsync(dist8, f->d_dist8, cells, d2d, s)) ||
+            (e = cudaMemcpyAsync(dist2, f->d_dist2, sizeof(uint32_t) * (size_t)nk * (size_t)sbc::d2_words(f->nv), d2d,
+                                 s)) ||
             (e = cudaMemcpyAsync(sigma, f->d_sigma, sizeof(int64_t) * cells, d2d, s)) ||
             (e = cudaMemcpyAsync(delta, f->d_delta, sizeof(double) * cells, d2d, s)) ||
             (e = cudaMemcpyAsync(bc, f->d_bc, sizeof(double) * f->nv, d2d, s)) ||
@@ -457,6 +462,7 @@ struct TrialState {
     {
         std::swap(f->d_dist, dist);
         std::swap(f->d_dist8, dist8);
+        std::swap(f->d_dist2, dist2);
         std::swap(f->d_sigma, sigma);
         std::swap(f->d_delta, delta);
         std::swap(f->d_bc, bc);
@@ -810,7 +816,7 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
     const size_t cells = (size_t)nk * (size_t)f->nv;
     cudaError_t e;
     if ((e = dev_alloc(&f->d_roots, nk)) || (e = dev_alloc(&f->d_dist, cells)) || (e = dev_alloc(&f->d_dist8, cells)) ||
-        (e = dev_alloc(&f->d_sigma, cells)) ||
+        (e = dev_alloc(&f->d_dist2, (size_t)nk * (size_t)sbc::d2_words(f->nv))) || (e = dev_alloc(&f->d_sigma, cells)) ||
         (e = dev_alloc(&f->d_delta, cells)) || (e = dev_alloc(&f->d_bc, f->nv)) || (e = dev_alloc(&f->d_worklist, nk)) ||
         (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, SBC_NCOUNTERS)) ||
         (e = dev_alloc(&f->d_mov, nk)) || (e = dev_alloc(&f->d_nmov, 2)) ||
@@ -828,7 +834,8 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
         sbc_forest_destroy(f);
         return cuda_fail(e, "sbc_forest_create roster allocation");
     }
-    f->state_bytes = (int64_t)(cells * 21 + f->nv * 8 + (f->d_roster ? roster_cells * 4 : 0));
+    f->state_bytes = (int64_t)(cells * 21 + (size_t)nk * sbc::d2_words(f->nv) * 4 + f->nv * 8 +
+                               (f->d_roster ? roster_cells * 4 : 0));
     f->workers_req = workers;
     int rc = alloc_scratch(f, variant);
     if (rc) {
@@ -859,6 +866,7 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_roots);
     dev_free(f->d_dist);
     dev_free(f->d_dist8);
+    dev_free(f->d_dist2);
     dev_free(f->d_sigma);
     dev_free(f->d_delta);
     dev_free(f->d_bc);
@@ -898,6 +906,7 @@ int sbc_static_init(sbc_forest* f)
     if (!f) return fail(SBC_ERR_ARG, "sbc_static_init: null");
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(sbc::launch_static(f));
+    CK(sbc::launch_dist2_rows(f, nullptr, nullptr));
     CK(sbc::launch_level_hist(f));
     CK(sbc::launch_roster_build(f));
     f->initialized = true;

@@ -169,6 +169,7 @@ struct sbc_forest {
     int64_t* d_roots = nullptr;
     int32_t* d_dist = nullptr;
     uint8_t* d_dist8 = nullptr;  // one-byte shadow of d_dist gathered by the walkers
+    uint32_t* d_dist2 = nullptr; // [nk][d2_words(nv)] two-bit shadow (dist mod 3) gathered by the update walks
     int64_t* d_sigma = nullptr;
     double* d_delta = nullptr;
     double* d_bc = nullptr;
@@ -336,6 +337,7 @@ inline ForestSlot forest_slot(const sbc_forest* f, int n)
     s.roots = f->d_roots;
     s.dist = f->d_dist;
     s.dist8 = f->d_dist8;
+    s.dist2 = f->d_dist2;
     s.sigma = f->d_sigma;
     s.delta = f->d_delta;
     s.bc = f->d_bc;
@@ -395,6 +397,8 @@ cudaError_t recompute_roots_wide(sbc_forest* f, const std::vector<int>& rows, co
 constexpr int kWideRecompute = 64;
 constexpr int64_t kWideRecomputeMinVertices = 32768;
 cudaError_t launch_level_hist_list(sbc_forest* f, const int* d_list, const int* d_nlist);
+// Two-bit rows of every root (or the listed roots) derived from their dist rows.
+cudaError_t launch_dist2_rows(sbc_forest* f, const int* d_list, const int* d_nlist);
 cudaError_t launch_roster_build_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 // Cost model and schedule (sbc_model.cu).
 cudaError_t launch_level_hist(sbc_forest* f);

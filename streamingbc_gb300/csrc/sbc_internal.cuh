@@ -25,6 +25,17 @@
 #define SBC_D8_DEEP 254
 #define SBC_D8_INF 255
 
+// Two-bit shadow of dist (dist2[K][d2_words(V)] 32-bit words, 16 vertices per
+// word, vertex k in bits 2*(k%16)..): dist mod 3 for a reachable vertex, 3
+// when unreachable.  Every neighbour of a reachable vertex at level L sits at
+// level L-1, L or L+1 (neighbours in a BFS tree differ by at most one level,
+// and share the vertex's component), so the code alone tells which.  The
+// walkers of the insertion update gather from it wherever the walked
+// vertices of a level all sit at one known level of a consistent labelling:
+// a root's gathered row is V/4 bytes (256 KB at 2^20 vertices, against 1 MB
+// for the one-byte shadow), so the rows of the roots in flight on every SM
+// stay in L2 and a hub's neighbour gathers stop missing to HBM.
+
 // Worker state bits (st[]).  Low bits: descent step + 1 (0 = not a descent
 // vertex).  MOVED: the vertex moved up a level.  ASC: touched by the ascent only.
 #define SBC_STEP_MASK 0x03ffffff
@@ -50,6 +61,7 @@ struct ForestSlot {
     const int64_t* roots;
     int32_t* dist;
     uint8_t* dist8;
+    uint32_t* dist2;    // [nk][d2_words(nv)] two-bit shadow
     int64_t* sigma;
     double* delta;
     double* bc;
@@ -154,9 +166,61 @@ __device__ __forceinline__ uint8_t enc_d8(int d)
     return d == SBC_INF ? (uint8_t)SBC_D8_INF : (d >= SBC_D8_DEEP ? (uint8_t)SBC_D8_DEEP : (uint8_t)d);
 }
 
+// 32-bit words of one root's two-bit row.
+__host__ __device__ __forceinline__ int64_t d2_words(int64_t nv) { return (nv + 15) / 16; }
+
+__device__ __forceinline__ unsigned enc_d2(int d) { return d == SBC_INF ? 3u : (unsigned)(d % 3); }
+
+// Level of a neighbour whose two-bit code is c, of a vertex at level Lw >= 0.
+__device__ __forceinline__ int dec_d2(unsigned c, int Lw)
+{
+    if (c == 3u) return SBC_INF;
+    const unsigned m = (unsigned)(Lw + 2) % 3u;  // code of level Lw - 1
+    return Lw - 1 + (int)((c + 3u - m) % 3u);
+}
+
+// Sets vertex k's code in a two-bit row to that of level d.  Only the thread
+// that owns k's new level writes k, and XOR touches k's two bits alone, so
+// concurrent updates of other vertices in the same word need no lock.
+__device__ __forceinline__ void set_d2(uint32_t* R, int k, int d)
+{
+    const int sh = (k & 15) * 2;
+    const unsigned old = (R[k >> 4] >> sh) & 3u;
+    const unsigned nw = enc_d2(d);
+    if (old != nw) atomicXor(&R[k >> 4], (old ^ nw) << sh);
+}
+
+// Where a walker reads its neighbours' distances: the two-bit row D2 when the
+// walked vertices all sit at level Lw of a consistent labelling, else the
+// one-byte row D8 (falling back to the int32 row D for levels >= 254).
+struct DistRow {
+    const int32_t* D;
+    const uint8_t* D8;
+    const uint32_t* D2;  // null: gather from D8
+    int Lw;
+};
+
 __device__ __forceinline__ void atomic_add_i64(int64_t* p, int64_t v)
 {
     atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
+}
+
+// Appends x to the queue q, whose length is the shared counter *cnt, for the
+// calling lanes whose `take` is set, with one shared atomic per warp instead
+// of one per appended vertex: the lanes converged here vote with a ballot,
+// the lowest taker reserves the warp's slots, and every taker writes at its
+// rank among them (frontier compaction by ballot and population count).
+__device__ __forceinline__ void warp_append(int* cnt, int32_t* q, int x, bool take)
+{
+    const unsigned act = __activemask();
+    const unsigned vote = __ballot_sync(act, take);
+    if (!take) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(vote) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(cnt, __popc(vote));
+    base = __shfl_sync(vote, base, leader);
+    q[base + __popc(vote & ((1u << lane) - 1u))] = x;
 }
 
 // Block-wide exclusive scan of one int per thread; returns the thread's prefix
@@ -244,6 +308,28 @@ __device__ __forceinline__ void walk_fetch(const DevGraph& G, const LbSmem<NT>& 
     }
 }
 
+// Distances of the walker's neighbours kk[u] (those >= 0) into dk[u]: every
+// gather of a round is issued before any is decoded.
+template <int ILP>
+__device__ __forceinline__ void gather_dist(const DistRow& dr, const int (&kk)[ILP], int (&dk)[ILP])
+{
+    if (dr.D2) {
+        unsigned w[ILP];
+#pragma unroll
+        for (int u = 0; u < ILP; ++u) w[u] = kk[u] >= 0 ? dr.D2[kk[u] >> 4] : 0u;
+#pragma unroll
+        for (int u = 0; u < ILP; ++u) dk[u] = dec_d2((w[u] >> ((kk[u] & 15) * 2)) & 3u, dr.Lw);
+    } else {
+#pragma unroll
+        for (int u = 0; u < ILP; ++u) dk[u] = kk[u] >= 0 ? (int)dr.D8[kk[u]] : 0;
+#pragma unroll
+        for (int u = 0; u < ILP; ++u) {
+            if (dk[u] == SBC_D8_INF) dk[u] = SBC_INF;
+            else if (dk[u] == SBC_D8_DEEP) dk[u] = dr.D[kk[u]];
+        }
+    }
+}
+
 // Edge-balanced walk over the neighbours of a vertex list given as up to two
 // ranges (l1[0..n1) then l2[0..n2)).  Vertices are taken NT at a time; each
 // thread runs prep(j, x, visible_degree) for its vertex, an exclusive scan of
@@ -255,7 +341,7 @@ __device__ __forceinline__ void walk_fetch(const DevGraph& G, const LbSmem<NT>& 
 // REF: the walked vertices and their degrees count as traversed in the
 // reference's sense (COUNT_TRAVERSALS); every walk counts its scanned slots.
 template <int NT, bool REF = true, int ILP = kEdgeIlp, class Prep, class Edge, class Post>
-__device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t* D, const uint8_t* D8,
+__device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const DistRow dr,
                                         const int32_t* l1, int n1, const int32_t* l2, int n2, LbSmem<NT>& sm,
                                         Prep prep, Edge edge, Post post)
 {
@@ -290,13 +376,7 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const int32_t*
         for (int e0 = t * per; e0 < total; e0 += NT * per) {
             int kk[ILP], jj[ILP], dk[ILP];
             walk_fetch<NT, ILP>(G, sm, cnt, total, e0, per, j, kk, jj);
-#pragma unroll
-            for (int u = 0; u < ILP; ++u) dk[u] = kk[u] >= 0 ? (int)D8[kk[u]] : 0;
-#pragma unroll
-            for (int u = 0; u < ILP; ++u) {
-                if (dk[u] == SBC_D8_INF) dk[u] = SBC_INF;
-                else if (dk[u] == SBC_D8_DEEP) dk[u] = D[kk[u]];
-            }
+            gather_dist<ILP>(dr, kk, dk);
 #pragma unroll
             for (int u = 0; u < ILP; ++u)
                 if (kk[u] >= 0) edge(jj[u], sm.x[jj[u]], kk[u], dk[u]);
@@ -324,7 +404,7 @@ struct NoPost {
 // walks whose edge test needs no distance.
 constexpr int kSumHit = 4;
 template <int NT, bool GATHER, int ILP = kEdgeIlp, class Prep, class Contrib, class Post>
-__device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const int32_t* D, const uint8_t* D8,
+__device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const DistRow dr,
                                             const int32_t* l1, int n1, LbSmem<NT>& sm, double* s_sum, int* s_hit,
                                             Prep prep, Contrib contrib, Post post)
 {
@@ -356,14 +436,11 @@ __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const int3
         for (int e0 = t * per; e0 < total; e0 += NT * per) {
             int kk[ILP], jj[ILP], dk[ILP];
             walk_fetch<NT, ILP>(G, sm, cnt, total, e0, per, j, kk, jj);
-#pragma unroll
-            for (int u = 0; u < ILP; ++u) dk[u] = (GATHER && kk[u] >= 0) ? (int)D8[kk[u]] : 0;
             if (GATHER) {
+                gather_dist<ILP>(dr, kk, dk);
+            } else {
 #pragma unroll
-                for (int u = 0; u < ILP; ++u) {
-                    if (dk[u] == SBC_D8_INF) dk[u] = SBC_INF;
-                    else if (dk[u] == SBC_D8_DEEP) dk[u] = D[kk[u]];
-                }
+                for (int u = 0; u < ILP; ++u) dk[u] = 0;
             }
 #pragma unroll
             for (int u = 0; u < ILP; ++u) {

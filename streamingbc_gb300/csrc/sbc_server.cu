@@ -18,6 +18,11 @@
 //               the graph's next batch (continuous batching).
 //   completion  a host callback queued behind each batch stamps its completion
 //               time; latency is completion minus the request's arrival time.
+//   tuning      optionally (sbc_server_set_tuning) a graph registered without
+//               a launch shape has its first batch applied through the
+//               launch-shape autotuner, and a graph's cost model is trained on
+//               the per-job costs logged over its first N insertions, after
+//               which its batches are scheduled by the model.
 //   eviction    an evicted graph's forest is checkpointed into host memory and
 //               its device memory freed; it rejoins the admission queue and,
 //               once it fits, is restored from the checkpoint (no static init)
@@ -55,6 +60,10 @@ struct ServerGraph {
     int64_t nv = 0, nk = 0;
     std::vector<int64_t> off, adj, roots;
     int variant = -1;
+    bool auto_variant = false;  // registered without a launch shape
+    bool tuned = false;         // first batch went through the autotuner
+    int model_phase = 0;        // 0 not started, 1 logging costs, 2 trained (model schedule)
+    int64_t logged = 0;         // insertions applied while logging
     int64_t footprint = 0;
     GraphState state = WAITING;
     bool release_requested = false;
@@ -78,6 +87,8 @@ struct sbc_server {
     int64_t budget = 0, used = 0;
     int max_batch = 1;
     int max_inflight = 0;  // batches on the device at once over all graphs (0 = no limit)
+    bool autotune = false;     // first batch of a graph without a launch shape through the tuner
+    int64_t train_n = 0;       // insertions of cost logging before a graph's model is trained (0 = off)
     int rr = 0;            // round-robin start of the launch scan
     Clock::time_point epoch;
     std::vector<std::unique_ptr<ServerGraph>> graphs;
@@ -104,11 +115,16 @@ int64_t footprint(int64_t nv, int64_t slots, int64_t nk, int variant, int sm_cou
 {
     const int64_t slack = slots + std::max<int64_t>(nv * 4, slots / 8);
     const int64_t graph = (nv + 1) * 8 + nv * 16 + slack * 8;
-    const int64_t state = nk * nv * 21 + nv * 8 + nk * (int64_t)sbc::kHistLevels * 4;
+    const int64_t state = nk * nv * 21 + nk * sbc::d2_words(nv) * 4 + nv * 8 + nk * (int64_t)sbc::kHistLevels * 4;
     int per_sm = std::max(1, sbc::update_workers_per_sm(variant));
     const int64_t workers = std::min<int64_t>((int64_t)per_sm * sm_count, nk);
     return graph + state + workers * (int64_t)WorkerScratch::per_worker(nv);
 }
+
+// The tuner times the first batch of at least this many requests (or of any
+// size when batches are capped below it): a shape tuned on a handful of
+// insertions would say little about full batches.
+constexpr int64_t kTuneMinBatch = 64;
 
 int default_variant(int64_t nv) { return nv <= 8192 ? 3 : (nv <= 262144 ? 5 : sbc::update_default_variant()); }
 
@@ -326,7 +342,33 @@ void scheduler(sbc_server* s)
                 u[i] = sg->batch[i].u;
                 v[i] = sg->batch[i].v;
             }
-            int rc = sbc_insert_batch_async(sg->f, (int64_t)u.size(), u.data(), v.data());
+            const int64_t n = (int64_t)u.size();
+            int rc = 0;
+            if (s->autotune && sg->auto_variant && !sg->tuned && (n >= kTuneMinBatch || s->max_batch < kTuneMinBatch)) {
+                // the tuner applies this batch after timing it under every shape
+                sg->tuned = true;
+                rc = sbc_forest_autotune(sg->f, n, u.data(), v.data(), 1, nullptr, nullptr, 0);
+            } else {
+                if (s->train_n > 0 && sg->model_phase == 0) {
+                    rc = sbc_cost_log_start(sg->f, std::min<int64_t>(s->train_n * sg->nk, (int64_t)1 << 26));
+                    sg->model_phase = 1;
+                }
+                if (!rc) rc = sbc_insert_batch_async(sg->f, n, u.data(), v.data());
+                if (!rc && sg->model_phase == 1 && (sg->logged += n) >= s->train_n) {
+                    // enough logged jobs: train (waits for this batch) and switch
+                    // the graph to the model's schedule
+                    int64_t samples = 0;
+                    sbc_model_stats ms;
+                    rc = sbc_cost_log_stop(sg->f, &samples);
+                    // minibatches of up to 4096 (a multiple of 128) of the 90 %
+                    // trained on; too few jobs logged: the static schedule stays
+                    const int64_t ntr = samples - (int64_t)((double)samples * 0.1);
+                    const int mb = (int)std::min<int64_t>(4096, ntr / 128 * 128);
+                    if (!rc && mb >= 128) rc = sbc_cost_model_train(sg->f, 4, mb, 2e-3, 0.1, 1, &ms);
+                    if (!rc && mb >= 128) rc = sbc_set_schedule(sg->f, SBC_SCHED_MODEL);
+                    sg->model_phase = 2;
+                }
+            }
             cudaError_t e = cudaSuccess;
             if (!rc) e = cudaLaunchHostFunc(sg->g->stream, on_batch_done, new DoneArg{s, sg});
             if (rc || e) {
@@ -359,6 +401,17 @@ int sbc_server_create(sbc_server** out, int device, int64_t hbm_budget_bytes, in
     s->epoch = Clock::now();
     s->sched = std::thread(scheduler, s);
     *out = s;
+    return SBC_OK;
+}
+
+int sbc_server_set_tuning(sbc_server* s, int autotune, int64_t train_insertions)
+{
+    if (!s || train_insertions < 0) return SBC_ERR_ARG;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->autotune = autotune != 0;
+        s->train_n = train_insertions;
+    }
     return SBC_OK;
 }
 
@@ -406,6 +459,7 @@ int sbc_server_add_graph(sbc_server* s, int64_t nv, const int64_t* off, const in
     sg->adj.assign(adj, adj + off[nv]);
     sg->roots.assign(roots, roots + nk);
     sg->variant = variant >= 0 ? variant : default_variant(nv);
+    sg->auto_variant = variant < 0;
     int sm_count = 0;
     if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, s->device)) return SBC_ERR_CUDA;
     sg->footprint = footprint(nv, off[nv], nk, sg->variant, sm_count);

@@ -90,19 +90,14 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         int L = 0, lo = 0, hi = 1;
         while (lo < hi) {
             lb_walk<NT>(
-                A.G, INT_MAX, D, D8, W.qd + lo, hi - lo, nullptr, 0, sm,
+                A.G, INT_MAX, DistRow{D, D8, nullptr, 0}, W.qd + lo, hi - lo, nullptr, 0, sm,
                 [&](int j, int x, int d) { s_sig[j] = Sg[x]; },
                 [&](int j, int x, int k, int dk) {
                     if (dk == SBC_INF) {
-                        int old = atomicCAS(&D[k], SBC_INF, L + 1);
-                        if (old == SBC_INF) {
-                            D8[k] = enc_d8(L + 1);
-                            int p = atomicAdd(&s_tail, 1);
-                            W.qd[p] = k;
-                            dk = L + 1;
-                        } else {
-                            dk = old;
-                        }
+                        const int old = atomicCAS(&D[k], SBC_INF, L + 1);
+                        if (old == SBC_INF) D8[k] = enc_d8(L + 1);
+                        warp_append(&s_tail, W.qd, k, old == SBC_INF);
+                        dk = old == SBC_INF ? L + 1 : old;
                     }
                     if (dk == L + 1) atomic_add_i64(&Sg[k], s_sig[j]);
                 },
@@ -123,7 +118,7 @@ __global__ void __launch_bounds__(NT) k_static(StaticArgs A)
         for (int l = nlev - 1; l >= 0; --l) {
             const int b0 = W.lvl[l], b1 = W.lvl[l + 1];
             lb_walk_sum<NT, true>(
-                A.G, INT_MAX, D, D8, W.qd + b0, b1 - b0, sm, s_acc, s_hit,
+                A.G, INT_MAX, DistRow{D, D8, nullptr, 0}, W.qd + b0, b1 - b0, sm, s_acc, s_hit,
                 [&](int j, int x, int d) {
                     s_hit[j] = 0;
                     atomicAdd(&sm.walked_v, 1ull);  // reference counters: walked vertex and its degree
@@ -165,6 +160,35 @@ __global__ void k_bc_colsum(const double* __restrict__ delta, const int64_t* __r
         }
         bc[v] = s;
     }
+}
+
+// Two-bit rows (dist mod 3, 3 = unreachable; 16 vertices per word) of every
+// root, or of the listed roots, from their int32 dist rows.  A thread packs
+// one word: 16 consecutive distances, 64 contiguous bytes.
+__global__ void k_dist2_rows(const int32_t* __restrict__ dist, int64_t nv, int nk, const int* __restrict__ list,
+                             const int* __restrict__ nlist, uint32_t* __restrict__ dist2)
+{
+    const int64_t nw = d2_words(nv);
+    const int64_t rows = list ? *nlist : nk;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows * nw;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = list ? list[i / nw] : i / nw;
+        const int64_t w = i % nw;
+        const int32_t* D = dist + r * nv;
+        uint32_t word = 0;
+        for (int t = 0; t < 16; ++t) {
+            const int64_t k = w * 16 + t;
+            word |= (k < nv ? enc_d2(D[k]) : 3u) << (2 * t);
+        }
+        dist2[r * nw + w] = word;
+    }
+}
+
+cudaError_t launch_dist2_rows(sbc_forest* f, const int* d_list, const int* d_nlist)
+{
+    k_dist2_rows<<<f->sm_count * 8, 256, 0, f->g->stream>>>(f->d_dist, f->nv, (int)f->nk, d_list, d_nlist,
+                                                             f->d_dist2);
+    return cudaGetLastError();
 }
 
 int static_workers_per_sm()

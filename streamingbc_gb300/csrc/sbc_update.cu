@@ -302,6 +302,7 @@ cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)
     }
     k_bc_rows<<<grid, 256, 0, s>>>(f->d_delta, f->d_roots, f->d_mov, f->d_nmov, f->nv, f->d_bc, 1.0);
     if ((e = cudaGetLastError())) return e;
+    if ((e = launch_dist2_rows(f, f->d_mov, f->d_nmov))) return e;
     if ((e = launch_level_hist_list(f, f->d_mov, f->d_nmov))) return e;
     return launch_roster_build_list(f, f->d_mov, f->d_nmov);
 }

@@ -40,6 +40,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
     const int64_t nv = A.G.nv;
     int32_t* D = A.dist + (size_t)r * nv;
     uint8_t* D8 = A.dist8 + (size_t)r * nv;
+    uint32_t* D2 = A.dist2 + (size_t)r * d2_words(nv);
     int64_t* S = A.sigma + (size_t)r * nv;
     double* Dl = A.delta + (size_t)r * nv;
     const int root = (int)A.roots[r];
@@ -64,21 +65,17 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
     while (lo < hi) {
         const int L = Lb + step;
         const int tag = step + 2;
+        // a re-levelling descent compares old distances far from L: one-byte row
         lb_walk<NT, true, ILP>(
-            A.G, g, D, D8, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
+            A.G, g, DistRow{D, D8, moving ? nullptr : D2, L}, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
             [&](int j, int x, int d) { sm.dp[j] = W.dp[x]; },
             [&](int j, int x, int k, int dk) {
                 if (moving ? (dk <= L) : (dk != L + 1)) return;
                 int s = W.st[k];
                 if (s == 0) {
-                    int old = atomicCAS(&W.st[k], 0, tag);
-                    if (old == 0) {
-                        int p = atomicAdd(&sm.qt, 1);
-                        W.qd[p] = k;
-                        s = tag;
-                    } else {
-                        s = old;
-                    }
+                    const int old = atomicCAS(&W.st[k], 0, tag);
+                    warp_append(&sm.qt, W.qd, k, old == 0);
+                    s = old == 0 ? tag : old;
                 }
                 if ((s & SBC_STEP_MASK) != tag) return;
                 atomic_add_i64(&W.dp[k], sm.dp[j]);
@@ -118,6 +115,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 }
                 D[k] = nl;
                 D8[k] = enc_d8(nl);
+                set_d2(D2, k, nl);
                 W.st[k] = s | SBC_MOVED;
             }
         }
@@ -175,11 +173,8 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
         const int sk = W.st[k];
         const bool kDown = (sk & SBC_STEP_MASK) != 0;
         if (!kDown && !(sk & SBC_ASC)) {
-            int old = atomicOr(&W.st[k], SBC_ASC);
-            if (!(old & SBC_ASC)) {
-                int p = atomicAdd(&sm.at, 1);
-                W.qa[p] = k;
-            }
+            const int old = atomicOr(&W.st[k], SBC_ASC);
+            warp_append(&sm.at, W.qa, k, !(old & SBC_ASC));
         }
         const bool fresh = kDown || (k == a && (sm.fl[j] & 2));
         atomicAdd(&W.acc[k], fresh ? sm.wn[j] : sm.wd[j]);
@@ -200,7 +195,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
     // gathering its distance and state.
     auto pull_walk = [&](const int32_t* plist, int pn) {
         lb_walk_sum<NT, false, ILP>(
-            A.G, g, D, D8, plist, pn, sm.lb, sm.wn, sm.fl,
+            A.G, g, DistRow{D, D8, nullptr, 0}, plist, pn, sm.lb, sm.wn, sm.fl,
             [&](int j, int y, int d) {
                 const int sy = W.st[y];
                 sm.fl[j] = ((sy & SBC_STEP_MASK) ? 1 : 0) | (y == a ? 2 : 0);
@@ -250,8 +245,8 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 const int sy = W.st[y];
                 const bool yDown = (sy & SBC_STEP_MASK) != 0;
                 if (!yDown && !(sy & SBC_ASC)) {
-                    int old = atomicOr(&W.st[y], SBC_ASC);
-                    if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = y;
+                    const int old = atomicOr(&W.st[y], SBC_ASC);
+                    warp_append(&sm.at, W.qa, y, !(old & SBC_ASC));
                 }
                 atomicAdd(&W.acc[y], (yDown || (y == a && x == b)) ? wn : wd);
             }
@@ -326,13 +321,14 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
             int nn1 = dn, nn2 = ua_hi - ua_lo;
             bool near = pull_ok;
             if (!pull_ok && !moving) {
-                lb_walk<NT, true, ILP>(A.G, g, D, D8, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb, prep_div,
+                lb_walk<NT, true, ILP>(A.G, g, DistRow{D, D8, D2, L}, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb,
+                                       prep_div,
                                        [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
                 probe_diverted();
             } else if (!pull_ok) {
                 const int same_lo = sm.st;
                 lb_walk<NT, true, ILP>(
-                    A.G, g, D, D8, dlist, dn, nullptr, 0, sm.lb, prep,
+                    A.G, g, DistRow{D, D8, D2, L}, dlist, dn, nullptr, 0, sm.lb, prep,
                     [&](int j, int x, int k, int dk) {
                         if (parent_edge(j, x, k, dk)) return;
                         if (!(sm.fl[j] & 1) || dk != L) return;
@@ -340,11 +336,8 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                         const int sk = W.st[k];
                         if (sk & SBC_STEP_MASK) return;
                         if (!(sk & SBC_ASC)) {
-                            int old = atomicOr(&W.st[k], SBC_ASC);
-                            if (!(old & SBC_ASC)) {
-                                int p = atomicAdd(&sm.st, 1);
-                                W.qs[p] = k;
-                            }
+                            const int old = atomicOr(&W.st[k], SBC_ASC);
+                            warp_append(&sm.st, W.qs, k, !(old & SBC_ASC));
                         }
                         atomicAdd(&W.acc[k], sm.wd[j] - sm.wn[j]);
                     },
@@ -360,7 +353,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                     nl2 = W.qs + same_lo;
                     nn2 = same_hi - same_lo;
                 } else {
-                    lb_walk<NT, true, ILP>(A.G, g, D, D8, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo,
+                    lb_walk<NT, true, ILP>(A.G, g, DistRow{D, D8, D2, L}, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo,
                                            same_hi - same_lo, sm.lb, prep_div,
                                            [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
                     probe_diverted();
@@ -431,7 +424,8 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                         pull_walk(A.G.col + rrow, rdeg);
                     } else {
                         const int nscan = sm.nscan, nprobe = sm.nprobe;
-                        lb_walk<NT, false, ILP>(A.G, g, D, D8, W.qs + qbase, nscan, nullptr, 0, sm.lb, prep_loaded,
+                        lb_walk<NT, false, ILP>(A.G, g, DistRow{D, D8, D2, L}, W.qs + qbase, nscan, nullptr, 0, sm.lb,
+                                                prep_loaded,
                                            [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
                         probe_parents(W.qs + nv - nprobe, nprobe, A.G.col + rrow, rdeg, false);
                     }

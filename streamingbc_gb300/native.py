@@ -137,6 +137,7 @@ def load(path: str = LIB_PATH):
         "sbc_server_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.c_int64, C.c_int]),
         "sbc_server_destroy": (C.c_int, [_vp]),
         "sbc_server_set_max_inflight": (C.c_int, [_vp, C.c_int]),
+        "sbc_server_set_tuning": (C.c_int, [_vp, C.c_int, C.c_int64]),
         "sbc_server_add_graph": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.c_int64, _i64p, C.c_int,
                                            C.POINTER(C.c_int)]),
         "sbc_server_graph_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), _i64p, _i64p, _i64p]),
@@ -699,7 +700,8 @@ class DeviceServer:
     """sbc_server: graphs resident on one device, insertion requests batched
     per graph as they arrive (admission by HBM footprint)."""
 
-    def __init__(self, budget_bytes: int, max_batch: int = 256, device: int = 0, max_inflight: int = 0):
+    def __init__(self, budget_bytes: int, max_batch: int = 256, device: int = 0, max_inflight: int = 0,
+                 autotune: bool = False, train_insertions: int = 0):
         self.lib = load()
         h = _vp()
         _check(self.lib.sbc_server_create(C.byref(h), int(device), int(budget_bytes), int(max_batch)))
@@ -707,6 +709,8 @@ class DeviceServer:
         self._shape = {}
         if max_inflight:
             self._rc(self.lib.sbc_server_set_max_inflight(self.h, int(max_inflight)))
+        if autotune or train_insertions:
+            self._rc(self.lib.sbc_server_set_tuning(self.h, 1 if autotune else 0, int(train_insertions)))
 
     def _rc(self, rc: int):
         if rc != 0:

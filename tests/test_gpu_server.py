@@ -56,6 +56,21 @@ def test_alone_unbatched_equals_reference(sbc_lib, mix):
     srv.close()
 
 
+def test_tuned_and_model_scheduled_serving_equals_alone(sbc_lib, mix):
+    """Every graph's first batch through the launch-shape tuner and its
+    batches after the first 100 insertions ordered by its own trained cost
+    model: each graph still ends where its stream alone ends."""
+    graphs, gid, pairs, t, refs = mix
+    srv = native.DeviceServer(budget_bytes=8 << 30, max_batch=64, autotune=True, train_insertions=100)
+    ids = [srv.add_graph(g, roots) for g, roots in graphs]
+    srv.play(gid, pairs, t)
+    srv.drain()
+    for i in ids:
+        _check(srv.read(i), refs[i])
+    assert srv.stats()["completed"] == len(gid)
+    srv.close()
+
+
 @pytest.mark.parametrize("max_batch,max_inflight", [(64, 0), (1, 1)])
 def test_mix_equals_alone(sbc_lib, mix, max_batch, max_inflight):
     """All graphs served together, with continuous batching or one insertion
