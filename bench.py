@@ -136,24 +136,29 @@ def kernel_source_hash() -> str:
 
 
 def traffic_estimate(workload, batch, alg_bytes_per_launch):
-    """DRAM bytes per k_update launch: profiles/k_update_<workload>_traffic.json
-    holds one small-case ncu capture (dram__bytes_read.sum +
-    dram__bytes_write.sum) with that launch's algorithmic bytes and the hash of
-    the kernel sources it ran; the ratio is applied to this run's algorithmic
-    bytes.  A capture of other sources, or none, gives null."""
-    path = os.path.join(ROOT, "profiles", f"k_update_{workload}_traffic.json")
+    """DRAM bytes per k_update launch, estimated from a small-case ncu capture.
+    profiles/k_update_traffic.json lists captures (dram__bytes_read.sum +
+    dram__bytes_write.sum of one launch, that launch's algorithmic bytes, the
+    hash of the kernel sources it ran and the bench workloads it stands for);
+    the DRAM/algorithmic ratio of the capture for this workload is applied to
+    this run's algorithmic bytes.  A capture of other kernel sources, or none,
+    gives null."""
+    path = os.path.join(ROOT, "profiles", "k_update_traffic.json")
     try:
         with open(path) as fh:
-            tj = json.load(fh)
-    except (OSError, ValueError):
-        return None, "no capture of this workload"
-    if tj.get("source_hash") != kernel_source_hash():
-        return None, (f"capture in {os.path.basename(path)} was taken with other kernel sources "
-                      f"({tj.get('source_hash')}); not used")
-    ratio = float(tj["dram_bytes_per_launch"]) / float(tj["alg_bytes_per_launch"])
-    return ratio * alg_bytes_per_launch, (f"small-case ncu capture ({tj.get('case')}): DRAM/algorithmic bytes "
-                                          f"{ratio:.3f}, applied to this run's algorithmic bytes; sources "
-                                          f"{tj['source_hash']}")
+            caps = json.load(fh)["captures"]
+    except (OSError, ValueError, KeyError):
+        return None, "no capture file"
+    cap = next((c for c in caps if workload in c.get("applies_to", [])), None)
+    if cap is None:
+        return None, f"no capture for {workload}"
+    if cap.get("source_hash") != kernel_source_hash():
+        return None, (f"capture ({cap.get('case')}) was taken with other kernel sources ({cap.get('source_hash')}); "
+                      f"not used")
+    ratio = float(cap["dram_bytes_per_launch"]) / float(cap["alg_bytes_per_launch"])
+    return ratio * alg_bytes_per_launch, (f"small-case ncu capture ({cap.get('case')}): DRAM/algorithmic bytes "
+                                          f"{ratio:.3f}, applied to this run's algorithmic bytes; kernel sources "
+                                          f"{cap['source_hash']}")
 
 
 def measured_peak():
@@ -933,6 +938,7 @@ def run_ours(args):
             deletions["cpu_port_recompute_s_per_deletion"] = cpu["static_init_s"]
 
     info = f.info()
+    variant_used = f.variant
     served = None
     if args.workload == "rmat20" and not args.no_served and world == 1:
         f.close()
@@ -949,7 +955,7 @@ def run_ours(args):
                                        f"insertions replicated, one BC all-reduce per e2e step)")
                                       if world > 1 else "single GPU",
                        "l2": f"per-root state {info['bytes'] / 1e9:.1f} GB on device >> 129 MB L2; no flush",
-                       "workers": info["workers"], "variant": f.variant, "autotune": tuned,
+                       "workers": info["workers"], "variant": variant_used, "autotune": tuned,
                        "static_init_s": static_s,
                        "graph_build_s": build_s,
                        "generate_s": gen_s,

@@ -6,6 +6,7 @@
 // (one direction for the directed form) after a duplicate check, and stamps the
 // slot with the insertion's index inside its batch (seq), so that a traversal
 // for insertion i of a batch sees only edges of insertions <= i.
+#include <climits>
 #include "sbc_host.h"
 #include "sbc_internal.cuh"
 
@@ -108,6 +109,122 @@ cudaError_t launch_stage(sbc_graph* g, int n)
     const int blocks = std::min((n + 255) / 256, 1024);
     k_stage_inputs<<<blocks < 1 ? 1 : blocks, 256, 0, g->stream>>>(g->d_src, g->d_ins, g->ins_capacity, n);
     return cudaGetLastError();
+}
+
+// After a batch's update: the slots it appended to a vertex (an unsorted tail
+// after the first nsort[x] slots, which are sorted by neighbour id) are merged
+// into the sorted prefix, so that edge tests (has_edge: binary search of the
+// prefix, then a scan of the tail) never scan more than the current batch's
+// appends -- without this a hub's tail grew by every insertion on it.  One
+// block per endpoint of an applied insertion; the first block to reach a
+// vertex claims it by swapping its deg0 for -1 (the seal that follows rewrites
+// deg0 = deg for the same endpoints; the update that read deg0 has finished).
+// The tail (at most kMergeTail slots per batch; a longer one is merged over
+// several batches) is sorted in shared memory; each tail value's final slot is
+// its rank among the tail plus its lower bound in the prefix; prefix values
+// move up by the number of tail values below them, in chunks from the end, so
+// no value is overwritten before it is read.  seq of the moved slots is not
+// read again (after the seal every slot is below deg0).
+constexpr int kMergeTail = 2048;
+constexpr int kMergeThreads = 256;
+constexpr int kMergeRun = 8;  // prefix values per thread per chunk
+
+__device__ __forceinline__ void merge_tail(const int64_t* __restrict__ row, const int32_t* __restrict__ deg,
+                                           int32_t* deg0, int32_t* nsort, int32_t* col, int x)
+{
+    __shared__ int s_tail[kMergeTail];
+    __shared__ int s_dst[kMergeTail];
+    __shared__ int s_claim;
+    const int tid = threadIdx.x;
+    if (tid == 0) s_claim = atomicExch(&deg0[x], -1);
+    __syncthreads();
+    if (s_claim < 0) return;  // another block merges x
+    const int ns = nsort[x];
+    const int t = min(deg[x] - ns, kMergeTail);
+    if (t <= 0) return;
+    const int64_t rx = row[x];
+    int P = 1;
+    while (P < t) P <<= 1;
+    for (int k = tid; k < P; k += kMergeThreads) s_tail[k] = k < t ? col[rx + ns + k] : INT_MAX;
+    __syncthreads();
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = tid; i < (P >> 1); i += kMergeThreads) {
+                const int lo = (i / stride) * 2 * stride + (i % stride);
+                const int hi = lo + stride;
+                const int a = s_tail[lo], b = s_tail[hi];
+                if ((a > b) == ((lo & size) == 0)) {
+                    s_tail[lo] = b;
+                    s_tail[hi] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int k = tid; k < t; k += kMergeThreads) {
+        const int v = s_tail[k];
+        int lo = 0, hi = ns;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (col[rx + mid] < v) lo = mid + 1;
+            else hi = mid;
+        }
+        s_dst[k] = lo + k;
+    }
+    __syncthreads();
+    const int first = s_dst[0];  // prefix values below it stay where they are
+    constexpr int kChunk = kMergeThreads * kMergeRun;
+    for (int c1 = ns; c1 > first; c1 -= kChunk) {
+        const int c0 = max(first, c1 - kChunk);
+        int val[kMergeRun], dst[kMergeRun];
+#pragma unroll
+        for (int r = 0; r < kMergeRun; ++r) {
+            const int idx = c0 + tid + r * kMergeThreads;
+            dst[r] = -1;
+            if (idx < c1) {
+                const int v = col[rx + idx];
+                int lo = 0, hi = t;  // tail values below v
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_tail[mid] < v) lo = mid + 1;
+                    else hi = mid;
+                }
+                val[r] = v;
+                dst[r] = idx + lo;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kMergeRun; ++r)
+            if (dst[r] >= 0) col[rx + dst[r]] = val[r];
+        __syncthreads();
+    }
+    for (int k = tid; k < t; k += kMergeThreads) col[rx + s_dst[k]] = s_tail[k];
+    if (tid == 0) nsort[x] = ns + t;
+}
+
+__global__ void __launch_bounds__(kMergeThreads) k_merge_tails(int n, const int32_t* __restrict__ iu,
+                                                               const int32_t* __restrict__ iv,
+                                                               const int32_t* __restrict__ ok,
+                                                               const int64_t* __restrict__ row,
+                                                               const int32_t* __restrict__ deg, int32_t* deg0,
+                                                               int32_t* nsort, int32_t* col)
+{
+    const int e = blockIdx.x;
+    const int i = e < n ? e : e - n;
+    if (ok[i] <= 0) return;
+    merge_tail(row, deg, deg0, nsort, col, e < n ? iu[i] : iv[i]);
+}
+
+// k_merge_tails over many graphs: blockIdx.y selects the graph.
+__global__ void __launch_bounds__(kMergeThreads) k_merge_tails_group(const __grid_constant__ GraphBatchSlots S)
+{
+    const GraphBatchSlot& b = S.slot[blockIdx.y];
+    const int e = blockIdx.x;
+    if (e >= 2 * b.n) return;
+    const int i = e < b.n ? e : e - b.n;
+    if (b.ok[i] <= 0) return;
+    merge_tail(b.row, b.deg, b.deg0, b.nsort, b.col, e < b.n ? b.iu[i] : b.iv[i]);
 }
 
 // After a batch: every appended slot becomes visible to all later traversals.
@@ -218,6 +335,9 @@ cudaError_t launch_seal(sbc_graph* g, int n)
     const int32_t* iu = g->d_ins;
     const int32_t* iv = g->d_ins + g->ins_capacity;
     const int32_t* ok = g->d_ins + 2 * g->ins_capacity;
+    if (n <= 0) return cudaSuccess;
+    k_merge_tails<<<2 * n, kMergeThreads, 0, g->stream>>>(n, iu, iv, ok, g->d_row, g->d_deg, g->d_deg0, g->d_nsort,
+                                                          g->d_col);
     k_seal<<<(n + 255) / 256, 256, 0, g->stream>>>(n, iu, iv, ok, g->d_deg, g->d_deg0);
     return cudaGetLastError();
 }
@@ -229,6 +349,7 @@ GraphBatchSlot graph_batch_slot(sbc_graph* g, int n)
     b.row = g->d_row;
     b.deg = g->d_deg;
     b.deg0 = g->d_deg0;
+    b.nsort = g->d_nsort;
     b.cap = g->d_cap;
     b.col = g->d_col;
     b.seq = g->d_seq;
@@ -252,6 +373,7 @@ cudaError_t launch_seal_group(const GraphBatchSlots& S, cudaStream_t s)
     int nmax = 0;
     for (int i = 0; i < S.count; ++i) nmax = std::max(nmax, S.slot[i].n);
     if (S.count <= 0 || nmax <= 0) return cudaSuccess;
+    k_merge_tails_group<<<dim3(2 * nmax, S.count), kMergeThreads, 0, s>>>(S);
     k_seal_group<<<dim3((nmax + 255) / 256, S.count), 256, 0, s>>>(S);
     return cudaGetLastError();
 }

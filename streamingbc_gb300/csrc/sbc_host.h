@@ -311,6 +311,7 @@ struct GraphBatchSlot {
     const int64_t* row;
     int32_t* deg;
     int32_t* deg0;
+    int32_t* nsort;
     const int32_t* cap;
     int32_t* col;
     int32_t* seq;

@@ -13,6 +13,7 @@
 //              int32 vertex queues (descent, ascent-up, ascent-same) plus level
 //              offsets.  Scratch is reset in O(touched) after every job.
 #pragma once
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -129,14 +130,22 @@ struct ScratchBase {
 };
 
 // Number of neighbour slots of x visible to the insertion with sequence g:
-// every slot below deg0[x], then appended slots while their seq <= g (slots are
-// appended in sequence order).
+// every slot below deg0[x], then the appended slots whose seq <= g.  Slots are
+// appended in sequence order, so those are a prefix of [deg0, deg): found by
+// binary search (a hub can take dozens of a batch's insertions; one dependent
+// load per appended slot was a long serial chain on every visit).
 __device__ __forceinline__ int vis_deg(const DevGraph& G, int x, int64_t rs, int g)
 {
-    int d0 = G.deg0[x];
-    int d = G.deg[x];
-    while (d0 < d && G.seq[rs + d0] <= g) ++d0;
-    return d0;
+    const int d0 = G.deg0[x];
+    const int d = G.deg[x];
+    if (d0 == d || g == INT_MAX) return d;
+    int lo = d0, hi = d;  // first slot in [d0, d) with seq > g
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (G.seq[rs + mid] <= g) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
 }
 
 // Is y among the first vx (visible) neighbours of x, whose slots start at rx?

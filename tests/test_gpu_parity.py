@@ -418,3 +418,36 @@ def test_rosters_on_deep_trees(sbc_lib, port_lib):
     assert tracked > 0
     f.close()
     dg.close()
+
+
+def test_adjacency_lists_stay_sorted_across_batches(sbc_lib, port_lib):
+    """The slots a batch appends are merged into each vertex's sorted list
+    after the batch: lists stay sorted, so edge lookups never scan more than
+    the current batch's appends.  A hub that takes more appends in one batch
+    than one merge covers (2,048) is merged over the next batches.  The state
+    stays the oracle's throughout."""
+    g = G.rmat(12, 8, seed=61)
+    roots = G.pick_roots(g.nv, 48, seed=61)
+    hub = int(np.argmax(np.diff(g.off)))
+    nbr = set(g.adj[g.off[hub]:g.off[hub + 1]].tolist())
+    star = np.array([(hub, y) for y in range(g.nv) if y != hub and y not in nbr][:2601], dtype=np.int64)
+    rest = G.rmat_insertions(g, 12, 300, seed=61)
+    rest = np.array([(u, v) for u, v in rest.tolist() if hub not in (u, v)], dtype=np.int64)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+
+    def sorted_lists():
+        off, adj = dg.to_csr()
+        return [v for v in range(g.nv) if np.any(np.diff(adj[off[v]:off[v + 1]]) <= 0)]
+
+    batches = [rest[:100], star[:2600], np.concatenate([star[2600:], rest[100:200]]), rest[200:]]
+    for k, batch in enumerate(batches):
+        for u, v in batch:
+            o.insert(int(u), int(v))
+        f.insert(batch)
+        check_state(f, o.level(), o.sigma(), o.bc())
+        # 2,600 appends on the hub: 2,048 merged after their batch, the rest
+        # after the next batch that appends to the hub
+        assert sorted_lists() == ([hub] if k == 1 else [])
