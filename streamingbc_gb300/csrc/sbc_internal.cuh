@@ -214,22 +214,29 @@ __device__ __forceinline__ void atomic_add_i64(int64_t* p, int64_t v)
     atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
 }
 
-// Appends x to the queue q, whose length is the shared counter *cnt, for the
-// calling lanes whose `take` is set, with one shared atomic per warp instead
+// warp_reserve: the slot index in a queue whose length is the shared counter
+// *cnt for each calling lane whose `take` is set (-1 for the others);
+// warp_append: appends x there.  One shared atomic per warp instead
 // of one per appended vertex: the lanes converged here vote with a ballot,
 // the lowest taker reserves the warp's slots, and every taker writes at its
 // rank among them (frontier compaction by ballot and population count).
-__device__ __forceinline__ void warp_append(int* cnt, int32_t* q, int x, bool take)
+__device__ __forceinline__ int warp_reserve(int* cnt, bool take)
 {
     const unsigned act = __activemask();
     const unsigned vote = __ballot_sync(act, take);
-    if (!take) return;
+    if (!take) return -1;
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(vote) - 1;
     int base = 0;
     if (lane == leader) base = atomicAdd(cnt, __popc(vote));
     base = __shfl_sync(vote, base, leader);
-    q[base + __popc(vote & ((1u << lane) - 1u))] = x;
+    return base + __popc(vote & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void warp_append(int* cnt, int32_t* q, int x, bool take)
+{
+    const int p = warp_reserve(cnt, take);
+    if (p >= 0) q[p] = x;
 }
 
 // Block-wide exclusive scan of one int per thread; returns the thread's prefix
@@ -467,16 +474,23 @@ __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const Dist
                 }
             }
         }
+        // The warp's largest running-sum source k0 (lanes without a sum
+        // hold -1) is summed with shuffles and added once; lanes whose sum
+        // belongs to another source add their own.  Sources are few and
+        // consecutive lanes mostly share one (a hub's slots), and a shared
+        // fp64 atomic per lane on the same address serialises.
         const unsigned full = 0xffffffffu;
-        const int k0 = __shfl_sync(full, cj, 0);
-        if (__all_sync(full, cj == k0) && k0 >= 0) {
+        const int k0 = __reduce_max_sync(full, cj);
+        if (k0 >= 0) {
+            double v = cj == k0 ? cs : 0.0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) cs += __shfl_xor_sync(full, cs, o);
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(full, v, o);
             if ((t & 31) == 0) {
-                atomicAdd(&s_sum[k0], cs);
+                atomicAdd(&s_sum[k0], v);
                 atomicOr(&s_hit[k0], kSumHit);
             }
-        } else if (cj >= 0) {
+        }
+        if (cj >= 0 && cj != k0) {
             atomicAdd(&s_sum[cj], cs);
             atomicOr(&s_hit[cj], kSumHit);
         }

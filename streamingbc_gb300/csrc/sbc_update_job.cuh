@@ -213,10 +213,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 W.acc[y] += sm.wn[j];  // y's only contributions at this level come from this walk
                 if (!(fl & 1)) {
                     int old = atomicOr(&W.st[y], SBC_ASC);
-                    if (!(old & SBC_ASC)) {
-                        int p = atomicAdd(&sm.at, 1);
-                        W.qa[p] = y;
-                    }
+                    warp_append(&sm.at, W.qa, y, !(old & SBC_ASC));
                 }
             });
     };
@@ -267,7 +264,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
         if (rcand && (long long)d > (long long)kProbeRatio * rcnt) {
             W.acc[x] = sm.wn[j];
             W.dp[x] = (int64_t)__double_as_longlong(sm.wd[j]);
-            W.lvl[nv + 1 - atomicAdd(&sm.nprobe, 1)] = x;
+            W.lvl[nv + 1 - warp_reserve(&sm.nprobe, true)] = x;
             atomicAdd(&sm.lb.walked_e, (unsigned long long)d);
             d = 0;
         }
@@ -388,11 +385,14 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                         root_sum += (rootDown || (root == a && x == b)) ? wn : wd;
                     } else if (L == 2) {
                         atomicOr(&W.bits[x >> 5], 1u << (x & 31));
-                        if ((long long)dx > (long long)kProbeRatio * rdeg) {
-                            W.qs[nv - 1 - atomicAdd(&sm.nprobe, 1)] = x;
+                        const bool probe = (long long)dx > (long long)kProbeRatio * rdeg;
+                        const int pp = warp_reserve(&sm.nprobe, probe);
+                        const int ps = warp_reserve(&sm.nscan, !probe);
+                        if (probe) {
+                            W.qs[nv - 1 - pp] = x;
                             mixed_cost += (long long)kProbeRatio * rdeg;
                         } else {
-                            W.qs[qbase + atomicAdd(&sm.nscan, 1)] = x;
+                            W.qs[qbase + ps] = x;
                             mixed_cost += dx;
                         }
                     }
