@@ -834,8 +834,22 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
         sbc_forest_destroy(f);
         return cuda_fail(e, "sbc_forest_create roster allocation");
     }
+    // level-2 parent masks (4 B per root per vertex) where they take at most a
+    // quarter of the free memory
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && cells * 4 <= free_b / 4) {
+        if ((e = dev_alloc(&f->d_l2mask, cells)) || (e = dev_alloc(&f->d_l1cand, (size_t)nk * sbc::kL1Max)) ||
+            (e = dev_alloc(&f->d_l1n, nk)) || (e = dev_alloc(&f->d_l2flag, nk)) || (e = dev_alloc(&f->d_l2list, nk)) ||
+            (e = dev_alloc(&f->d_l2cnt, 1))) {
+            sbc_forest_destroy(f);
+            return cuda_fail(e, "sbc_forest_create mask allocation");
+        }
+        CK(cudaMemsetAsync(f->d_l1n, 0xff, sizeof(int32_t) * nk, g->stream));  // -1: no masks until built
+        CK(cudaMemsetAsync(f->d_l2flag, 0, sizeof(int32_t) * nk, g->stream));
+        CK(cudaMemsetAsync(f->d_l2cnt, 0, sizeof(int32_t), g->stream));
+    }
     f->state_bytes = (int64_t)(cells * 21 + (size_t)nk * sbc::d2_words(f->nv) * 4 + f->nv * 8 +
-                               (f->d_roster ? roster_cells * 4 : 0));
+                               (f->d_roster ? roster_cells * 4 : 0) + (f->d_l2mask ? cells * 4 : 0));
     f->workers_req = workers;
     int rc = alloc_scratch(f, variant);
     if (rc) {
@@ -867,6 +881,12 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_dist);
     dev_free(f->d_dist8);
     dev_free(f->d_dist2);
+    dev_free(f->d_l2mask);
+    dev_free(f->d_l1cand);
+    dev_free(f->d_l1n);
+    dev_free(f->d_l2flag);
+    dev_free(f->d_l2list);
+    dev_free(f->d_l2cnt);
     dev_free(f->d_sigma);
     dev_free(f->d_delta);
     dev_free(f->d_bc);
@@ -907,6 +927,7 @@ int sbc_static_init(sbc_forest* f)
     if (use_device(f->g->device)) return SBC_ERR_CUDA;
     CK(sbc::launch_static(f));
     CK(sbc::launch_dist2_rows(f, nullptr, nullptr));
+    CK(sbc::launch_l2mask_build_all(f));
     CK(sbc::launch_level_hist(f));
     CK(sbc::launch_roster_build(f));
     f->initialized = true;

@@ -157,6 +157,7 @@ int sbc_checkpoint_restore(const sbc_checkpoint* c, int variant, sbc_graph** g_o
     sbc::k_dist8_rows<<<f->sm_count * 8, 256, 0, s>>>(f->d_dist, f->d_dist8, cells);
     if ((rc = ck(cudaGetLastError(), "one-byte distances")) ||
         (rc = ck(sbc::launch_dist2_rows(f, nullptr, nullptr), "two-bit distances")) ||
+        (rc = ck(sbc::launch_l2mask_build_all(f), "level-2 masks")) ||
         (rc = ck(sbc::launch_level_hist(f), "level histograms")) ||
         (rc = ck(sbc::launch_roster_build(f), "rosters")) || (rc = ck(cudaStreamSynchronize(s), "restore"))) {
         sbc_forest_destroy(f);

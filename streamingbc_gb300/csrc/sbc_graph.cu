@@ -327,6 +327,7 @@ cudaError_t launch_append(sbc_graph* g, int n, bool directed)
     int32_t* ok = g->d_ins + 2 * g->ins_capacity;
     k_append<<<1, 32, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_cap, g->d_col, g->d_seq, n, iu, iv, ok,
                                       directed ? 1 : 0, g->d_err);
+    g->last_directed = directed;
     return cudaGetLastError();
 }
 
@@ -339,7 +340,9 @@ cudaError_t launch_seal(sbc_graph* g, int n)
     k_merge_tails<<<2 * n, kMergeThreads, 0, g->stream>>>(n, iu, iv, ok, g->d_row, g->d_deg, g->d_deg0, g->d_nsort,
                                                           g->d_col);
     k_seal<<<(n + 255) / 256, 256, 0, g->stream>>>(n, iu, iv, ok, g->d_deg, g->d_deg0);
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e) return e;
+    return launch_l2mask_insert(g, n, g->last_directed);
 }
 
 GraphBatchSlot graph_batch_slot(sbc_graph* g, int n)
@@ -382,7 +385,9 @@ cudaError_t launch_remove(sbc_graph* g, int u, int v, bool directed, int* d_res)
 {
     k_remove<<<1, 32, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_deg0, g->d_nsort, g->d_col, g->d_seq, u, v,
                                       directed ? 1 : 0, d_res);
-    return cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e) return e;
+    return launch_l2mask_remove(g, u, v, directed, d_res);
 }
 
 cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq)

@@ -152,7 +152,13 @@ cudaError_t launch_group_update(sbc_group* G, const int* counts, unsigned steps)
         for (int i = 0; i < ns; ++i)
             if ((e = launch_roster_compact(G->members[i], s))) return e;
     }
-    if (steps & GROUP_SEAL) return launch_seal_group(B, s);
+    if (steps & GROUP_SEAL) {
+        if ((e = launch_seal_group(B, s))) return e;
+        // level-2 masks of every forest on the members' graphs
+        for (int i = 0; i < ns; ++i)
+            for (sbc_forest* f : G->members[i]->g->forests)
+                if ((e = launch_l2mask_insert_forest(f, counts[i], false, s))) return e;
+    }
     return cudaSuccess;
 }
 

@@ -146,6 +146,7 @@ struct sbc_graph {
     int64_t repacks = 0;
     // forests bound to this graph; destroying the graph detaches them
     std::vector<sbc_forest*> forests;
+    bool last_directed = false;  // the staged insertions were appended one direction only
 
     sbc::DevGraph dev() const
     {
@@ -184,6 +185,16 @@ struct sbc_forest {
     int32_t* d_roster = nullptr;   // [nk][kRosterLevels][kRosterCap] small-level members (null: no rosters)
     int32_t* d_roster_n = nullptr;
     int32_t* d_roster_dirty = nullptr;
+    // level-2 parent masks (null when they would not fit): [nk][nv] masks,
+    // [nk][kL1Max] root neighbours, [nk] their counts, and the roots whose
+    // masks must be rebuilt after the current graph change ([nk] flags,
+    // [nk] list, [1] count)
+    uint32_t* d_l2mask = nullptr;
+    int32_t* d_l1cand = nullptr;
+    int32_t* d_l1n = nullptr;
+    int32_t* d_l2flag = nullptr;
+    int32_t* d_l2list = nullptr;
+    int32_t* d_l2cnt = nullptr;
     CostModel* model = nullptr;    // allocated by the first cost-model call
     int schedule = 0;              // root order of a batch: 0 static (classify order), 1 cost model
     int64_t state_bytes = 0;
@@ -352,6 +363,9 @@ inline ForestSlot forest_slot(const sbc_forest* f, int n)
     s.roster = f->d_roster;
     s.roster_n = f->d_roster_n;
     s.roster_dirty = f->d_roster_dirty;
+    s.l2mask = f->d_l2mask;
+    s.l1cand = f->d_l1cand;
+    s.l1n = f->d_l1n;
     return s;
 }
 
@@ -400,6 +414,14 @@ constexpr int64_t kWideRecomputeMinVertices = 32768;
 cudaError_t launch_level_hist_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 // Two-bit rows of every root (or the listed roots) derived from their dist rows.
 cudaError_t launch_dist2_rows(sbc_forest* f, const int* d_list, const int* d_nlist);
+// Level-2 parent masks of every root (after static init or a restore).
+cudaError_t launch_l2mask_build_all(sbc_forest* f);
+// Masks of every forest of g after the n insertions staged in g were appended
+// (directed: only the u -> v slots), and after the removal of (u, v) when
+// *d_removed (directed: the u -> v slot only).
+cudaError_t launch_l2mask_insert(sbc_graph* g, int n, bool directed);
+cudaError_t launch_l2mask_insert_forest(sbc_forest* f, int n, bool directed, cudaStream_t s);
+cudaError_t launch_l2mask_remove(sbc_graph* g, int u, int v, bool directed, const int* d_removed);
 cudaError_t launch_roster_build_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 // Cost model and schedule (sbc_model.cu).
 cudaError_t launch_level_hist(sbc_forest* f);

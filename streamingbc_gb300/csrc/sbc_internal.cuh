@@ -76,7 +76,21 @@ struct ForestSlot {
     int32_t* roster;    // [nk][kRosterLevels][kRosterCap] members of small levels, or null
     int32_t* roster_n;  // [nk][kRosterLevels] entries (> kRosterCap: level not tracked)
     int32_t* roster_dirty;  // [nk][kRosterLevels] 1 once an entry went stale
+    const uint32_t* l2mask; // [nk][nv] level-2 parent masks (see kL1Max), or null
+    const int32_t* l1cand;  // [nk][kL1Max] the root's neighbours, bit i of a mask = l1cand[i]
+    const int32_t* l1n;     // [nk] their count, -1 where the root has no masks
 };
+
+// Level-2 parent masks.  The parents of a vertex x at level 2 of root r's
+// tree are its neighbours at level 1, i.e. N(x) ∩ N(r) -- a relation of the
+// graph alone, whatever the BFS state.  For a root with at most kL1Max
+// neighbours l1cand[r][0..n), mask[r][x] holds bit i set iff l1cand[r][i] is
+// adjacent to x through an edge that existed when the current batch began
+// (built after static init, extended by every batch's insertions and cleared
+// by deletions; rebuilt when an edge of the root itself changes).  A level-2
+// ascent step then finds each vertex's parents with one load instead of
+// scanning adjacency lists.
+constexpr int kL1Max = 32;
 
 // Levels tracked by the per-root level histograms (deeper levels share the last bucket).
 constexpr int kHistLevels = 64;

@@ -109,13 +109,14 @@ struct sbc_server {
 namespace {
 
 // Device bytes a graph will hold once admitted: slack CSR (row, deg, deg0,
-// nsort, cap, col, seq), per-root state (dist, dist8, sigma, delta), BC,
+// nsort, cap, col, seq), per-root state (dist, dist8, dist2, level-2 masks,
+// sigma, delta), BC,
 // level histograms and the update workers' scratch for its launch shape.
 int64_t footprint(int64_t nv, int64_t slots, int64_t nk, int variant, int sm_count)
 {
     const int64_t slack = slots + std::max<int64_t>(nv * 4, slots / 8);
     const int64_t graph = (nv + 1) * 8 + nv * 16 + slack * 8;
-    const int64_t state = nk * nv * 21 + nk * sbc::d2_words(nv) * 4 + nv * 8 + nk * (int64_t)sbc::kHistLevels * 4;
+    const int64_t state = nk * nv * 25 + nk * sbc::d2_words(nv) * 4 + nv * 8 + nk * (int64_t)sbc::kHistLevels * 4;
     int per_sm = std::max(1, sbc::update_workers_per_sm(variant));
     const int64_t workers = std::min<int64_t>((int64_t)per_sm * sm_count, nk);
     return graph + state + workers * (int64_t)WorkerScratch::per_worker(nv);

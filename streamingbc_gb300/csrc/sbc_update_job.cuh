@@ -18,6 +18,7 @@ struct UpdSmem {
     long long part[3 * (NT / 32) + 3];
     int item, qt, at, st;
     int nscan, nprobe;  // level-2 vertices whose parents are found by scan / by probe
+    int mask_ok;        // the current root's level-2 masks hold for this batch
     unsigned long long c1, c2;  // case-1 / case-2 jobs of this CTA (written by thread 0)
 };
 
@@ -38,6 +39,9 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                                         int a, int b, bool moving, int g, bool del = false)
 {
     const int64_t nv = A.G.nv;
+    const uint32_t* M2 = sm.mask_ok ? A.l2mask + (size_t)r * nv : nullptr;
+    const int32_t* C1 = sm.mask_ok ? A.l1cand + (size_t)r * kL1Max : nullptr;
+    const int n1 = sm.mask_ok ? A.l1n[r] : 0;
     int32_t* D = A.dist + (size_t)r * nv;
     uint8_t* D8 = A.dist8 + (size_t)r * nv;
     uint32_t* D2 = A.dist2 + (size_t)r * d2_words(nv);
@@ -383,6 +387,29 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                     push_cost += dx;
                     if (L == 1) {
                         root_sum += (rootDown || (root == a && x == b)) ? wn : wd;
+                    } else if (L == 2 && M2) {
+                        // parents from the mask (edges older than the batch),
+                        // plus this batch's edges visible here that reach a root
+                        // neighbour (level 1)
+                        unsigned m = M2[x];
+                        const int64_t rx = A.G.row[x];
+                        for (int sl = A.G.deg0[x]; sl < dx; ++sl) {
+                            const int z = A.G.col[rx + sl];
+                            if (D8[z] == 1)
+                                for (int q = 0; q < n1; ++q)
+                                    if (C1[q] == z) m |= 1u << q;
+                        }
+                        while (m) {
+                            const int q = __ffs(m) - 1;
+                            m &= m - 1;
+                            const int y = C1[q];
+                            const bool yDown = (W.st[y] & SBC_STEP_MASK) != 0;
+                            if (!yDown) {
+                                const int old = atomicOr(&W.st[y], SBC_ASC);
+                                warp_append(&sm.at, W.qa, y, !(old & SBC_ASC));
+                            }
+                            atomicAdd(&W.acc[y], (yDown || (y == a && x == b)) ? wn : wd);
+                        }
                     } else if (L == 2) {
                         atomicOr(&W.bits[x >> 5], 1u << (x & 31));
                         const bool probe = (long long)dx > (long long)kProbeRatio * rdeg;
@@ -411,6 +438,8 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                         }
                     }
                     __syncthreads();
+                } else if (L == 2 && nn1 + nn2 > 0 && M2) {
+                    __syncthreads();  // every parent took its share in the commit loop
                 } else if (L == 2 && nn1 + nn2 > 0) {
                     if (pull2_cost < 0) {
                         long long c = 0;
@@ -473,6 +502,18 @@ __device__ __forceinline__ void process_root(const ForestSlot& A, UpdSmem<NT>& s
                                              bool all_visible)
 {
     const int32_t* D = A.dist + (size_t)r * A.G.nv;
+    // level-2 masks hold for the whole batch unless one of its insertions
+    // changes the root's own neighbour list
+    bool mk = A.l2mask && A.l1n[r] >= 0;
+    if (mk) {
+        const int root = (int)A.roots[r];
+        int hit = 0;
+        for (int i = threadIdx.x; i < A.nins; i += NT)
+            if (A.ins_ok[i] > 0 && (A.ins_u[i] == root || A.ins_v[i] == root)) hit = 1;
+        mk = !__syncthreads_or(hit);
+    }
+    if (threadIdx.x == 0) sm.mask_ok = mk ? 1 : 0;
+    __syncthreads();
     for (int i = 0; i < A.nins; ++i) {
         if (A.ins_ok[i] <= 0) continue;
         const int u = A.ins_u[i], v = A.ins_v[i];
@@ -502,7 +543,12 @@ __device__ __forceinline__ void process_deletion(const ForestSlot& A, UpdSmem<NT
     const int32_t* D = A.dist + (size_t)r * A.G.nv;
     const int du = D[u], dv = D[v];
     if (du == dv) return;
-    if (threadIdx.x == 0) sm.c1 += 1;
+    // the masks were brought up to date with the removal before this launch
+    if (threadIdx.x == 0) {
+        sm.c1 += 1;
+        sm.mask_ok = (A.l2mask && A.l1n[r] >= 0) ? 1 : 0;
+    }
+    __syncthreads();
     run_job<NT, ILP>(A, sm, W, r, du < dv ? u : v, du < dv ? v : u, false, INT_MAX, true);
 }
 

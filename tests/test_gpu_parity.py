@@ -451,3 +451,63 @@ def test_adjacency_lists_stay_sorted_across_batches(sbc_lib, port_lib):
         # 2,600 appends on the hub: 2,048 merged after their batch, the rest
         # after the next batch that appends to the hub
         assert sorted_lists() == ([hub] if k == 1 else [])
+
+
+def test_level2_masks_follow_graph_changes(sbc_lib, port_lib):
+    """Level-2 ascents of roots with at most 32 neighbours find parents from
+    per-root masks kept up to date with the graph.  Insertions and deletions
+    at the roots themselves (the mask is rebuilt) and at root neighbours (bits
+    set and cleared), in batches and one at a time, interleaved: the state
+    stays the oracle's."""
+    g = G.rmat(9, 8, seed=71)
+    deg = np.diff(g.off)
+    roots = np.array([v for v in G.pick_roots(g.nv, 200, seed=71) if 0 < deg[v] <= 32][:48], dtype=np.int64)
+    rng = np.random.default_rng(71)
+    adj = {v: set(g.adj[g.off[v]:g.off[v + 1]].tolist()) for v in range(g.nv)}
+
+    def new_edges(anchors, count):
+        out = set()
+        while len(out) < count:
+            a = int(rng.choice(anchors))
+            b = int(rng.integers(g.nv))
+            if a != b and b not in adj[a] and (min(a, b), max(a, b)) not in out:
+                out.add((min(a, b), max(a, b)))
+        for a, b in out:
+            adj[a].add(b)
+            adj[b].add(a)
+        return np.array(sorted(out), dtype=np.int64)
+
+    def old_edges(anchors, count):
+        out = []
+        for a in rng.permutation(anchors):
+            a = int(a)
+            if adj[a] and len(out) < count:
+                b = int(rng.choice(sorted(adj[a])))
+                adj[a].discard(b)
+                adj[b].discard(a)
+                out.append((a, b))
+        return np.array(out, dtype=np.int64)
+
+    nbrs = np.array(sorted({int(y) for r in roots for y in adj[int(r)]}), dtype=np.int64)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg, f = make(g.nv, g.off, g.adj, roots)
+    f.static_init()
+    steps = [("ins", new_edges(roots[:6], 6)), ("ins", new_edges(nbrs, 40)), ("del", old_edges(nbrs, 5)),
+             ("del", old_edges(roots[6:10], 3)), ("ins", np.concatenate([new_edges(roots[10:14], 4),
+                                                                          new_edges(nbrs, 30)])),
+             ("ins1", new_edges(nbrs, 5))]
+    for kind, edges in steps:
+        if kind == "del":
+            for u, v in edges:
+                assert o.delete(int(u), int(v))
+            f.delete(edges)
+        else:
+            for u, v in edges:
+                o.insert(int(u), int(v))
+            if kind == "ins1":
+                for e in edges:
+                    f.insert([e])
+            else:
+                f.insert(edges)
+        check_state(f, o.level(), o.sigma(), o.bc())
