@@ -135,23 +135,24 @@ def kernel_source_hash() -> str:
     return h.hexdigest()[:16]
 
 
-def traffic_estimate(workload, batch, alg_bytes_per_launch):
-    """DRAM bytes per k_update launch, estimated from a small-case ncu capture.
+def traffic_estimate(workload, batch, alg_bytes_per_launch, roots=None, workers=None):
+    """DRAM bytes per k_update launch from an ncu capture of the same case.
     profiles/k_update_traffic.json lists captures (dram__bytes_read.sum +
     dram__bytes_write.sum of one launch, that launch's algorithmic bytes, the
-    hash of the kernel sources it ran and the bench workloads it stands for);
-    the DRAM/algorithmic ratio of the capture for this workload is applied to
-    this run's algorithmic bytes.  A capture of other kernel sources, or none,
-    gives null."""
+    hash of the kernel sources it ran and the case -- workload, roots, workers,
+    batch -- it measured); the DRAM/algorithmic ratio of the capture of this
+    case is applied to this run's algorithmic bytes.  No capture of this case,
+    or one of other kernel sources, gives null."""
     path = os.path.join(ROOT, "profiles", "k_update_traffic.json")
     try:
         with open(path) as fh:
             caps = json.load(fh)["captures"]
     except (OSError, ValueError, KeyError):
         return None, "no capture file"
-    cap = next((c for c in caps if workload in c.get("applies_to", [])), None)
+    case = f"{workload}/{roots} roots/{workers} workers/batch {batch}"
+    cap = next((c for c in caps if case in c.get("applies_to", [])), None)
     if cap is None:
-        return None, f"no capture for {workload}"
+        return None, f"no ncu capture of this case ({case}); profiles/k_update_traffic.json lists the captured ones"
     if cap.get("source_hash") != kernel_source_hash():
         return None, (f"capture ({cap.get('case')}) was taken with other kernel sources ({cap.get('source_hash')}); "
                       f"not used")
@@ -871,7 +872,8 @@ def run_ours(args):
     upd_ms = prof["update_ms"] / upd_launches
     achieved = (alg_bytes / upd_launches) / (upd_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic, traffic_note = traffic_estimate(args.workload, B, alg_bytes / upd_launches)
+    traffic, traffic_note = traffic_estimate(args.workload, B, alg_bytes / upd_launches, len(roots),
+                                             f.info()["workers"])
 
     # ---------------- plain path: one insertion per call ----------------
     plain = None

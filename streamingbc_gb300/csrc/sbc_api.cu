@@ -819,7 +819,8 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
         (e = dev_alloc(&f->d_dist2, (size_t)nk * (size_t)sbc::d2_words(f->nv))) || (e = dev_alloc(&f->d_sigma, cells)) ||
         (e = dev_alloc(&f->d_delta, cells)) || (e = dev_alloc(&f->d_bc, f->nv)) || (e = dev_alloc(&f->d_worklist, nk)) ||
         (e = dev_alloc(&f->d_nwork, 2)) || (e = dev_alloc(&f->d_counters, SBC_NCOUNTERS)) ||
-        (e = dev_alloc(&f->d_mov, nk)) || (e = dev_alloc(&f->d_nmov, 2)) ||
+        (e = dev_alloc(&f->d_mov, nk)) || (e = dev_alloc(&f->d_nmov, 2)) || (e = dev_alloc(&f->d_dirty, nk)) ||
+        (e = dev_alloc(&f->d_dlist, nk)) || (e = dev_alloc(&f->d_dcnt, 1)) ||
         (e = dev_alloc(&f->d_lvlhist, (size_t)nk * sbc::kHistLevels))) {
         sbc_forest_destroy(f);
         return cuda_fail(e, "sbc_forest_create state allocation");
@@ -857,6 +858,8 @@ int sbc_forest_create_ex(sbc_forest** out, sbc_graph* g, int64_t nk, const int64
         return rc;
     }
     CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
+    CK(cudaMemsetAsync(f->d_dirty, 0, sizeof(int) * nk, g->stream));
+    CK(cudaMemsetAsync(f->d_dcnt, 0, sizeof(int), g->stream));
     CK(cudaMemcpyAsync(f->d_roots, roots, sizeof(int64_t) * nk, cudaMemcpyHostToDevice, g->stream));
     CK(f->prof_init());
     CK(cudaEventCreate(&f->t0));
@@ -895,6 +898,9 @@ int sbc_forest_destroy(sbc_forest* f)
     dev_free(f->d_counters);
     dev_free(f->d_lvlhist);
     dev_free(f->d_mov);
+    dev_free(f->d_dirty);
+    dev_free(f->d_dlist);
+    dev_free(f->d_dcnt);
     dev_free(f->d_wide);
     dev_free(f->d_nmov);
     dev_free(f->d_roster);
@@ -1216,13 +1222,16 @@ int sbc_delete_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* 
     if (rc) return rc;
     int32_t* codes = g->d_ins + 2 * g->ins_capacity;
     if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
-    // one deletion at a time, in order: remove the edge, then update every root
+    // one deletion at a time, in order: remove the edge, then update every
+    // root that keeps a parent of the deeper endpoint; roots that lose it are
+    // recomputed once, on the final graph, after the last deletion
     for (int64_t i = 0; i < n; ++i) {
         const bool valid = u[i] >= 0 && v[i] >= 0 && u[i] < g->nv && v[i] < g->nv && u[i] != v[i];
         const int a = valid ? (int)u[i] : -1, b = valid ? (int)v[i] : -1;
         CK(sbc::launch_remove(g, a, b, false, codes + i));
-        if (valid) CK(sbc::launch_delete(f, a, b, codes + i));
+        if (valid) CK(sbc::launch_delete_step(f, a, b, codes + i));
     }
+    CK(sbc::launch_delete_finish(f));
     if (stats) return deletion_stats(f, n, codes, stats);
     CK(cudaStreamSynchronize(g->stream));
     return SBC_OK;

@@ -202,6 +202,11 @@ struct sbc_forest {
     int* d_worklist = nullptr;
     int* d_mov = nullptr;     // [nk] roots a deletion leaves without a parent of the deeper endpoint
     int* d_nmov = nullptr;    // [2]: their count, work counter
+    // roots left for a recompute at the end of a deletion batch: [nk] flags,
+    // [nk] list, [1] count
+    int* d_dirty = nullptr;
+    int* d_dlist = nullptr;
+    int* d_dcnt = nullptr;
     int* d_wide = nullptr;    // [3 * kWideRecompute]: BFS lengths and level ranges of the wide recompute
     int* d_res = nullptr;     // [1] result of the last edge removal
     int* d_nwork = nullptr;   // [1]
@@ -399,6 +404,12 @@ cudaError_t launch_remove(sbc_graph* g, int u, int v, bool directed, int* d_res)
 // (*d_removed must be 1, else nothing is done): roots that keep a parent of the
 // deeper endpoint get the sigma-decrease descent and ascent; the others are
 // recomputed from scratch, their old dependencies taken out of BC first.
+// One deletion of a batch (edge already removed when *d_removed == 1): roots
+// that keep a parent of the deeper endpoint are updated, the others take
+// their BC row out and are left for launch_delete_finish, which recomputes
+// them once on the batch's final graph and puts their rows back.
+cudaError_t launch_delete_step(sbc_forest* f, int u, int v, const int* d_removed);
+cudaError_t launch_delete_finish(sbc_forest* f);
 cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed);
 // Static recompute of the roots listed (device list and count) or, with a
 // null list, of all roots.

@@ -166,12 +166,14 @@ constexpr int kDefaultVariant = 7;
 // its subtree moves down -- recompute list (the reference's split,
 // src/streamingbc.c:300-345).
 __global__ void k_classify_delete(const int32_t* __restrict__ dist, int64_t nv, int nk, DevGraph G, int u, int v,
-                                  const int* __restrict__ removed, int* __restrict__ adj, int* __restrict__ nadj,
-                                  int* __restrict__ mov, int* __restrict__ nmov, unsigned long long* counters)
+                                  const int* __restrict__ removed, const int* __restrict__ dirty,
+                                  int* __restrict__ adj, int* __restrict__ nadj, int* __restrict__ mov,
+                                  int* __restrict__ nmov, unsigned long long* counters)
 {
     const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (r >= nk || *removed != 1) return;
+    // a root left for the batch's final recompute is no longer followed
+    if (r >= nk || *removed != 1 || dirty[r]) return;
     const int32_t* D = dist + (size_t)r * nv;
     const int du = D[u], dv = D[v];
     if (du == dv) return;
@@ -256,7 +258,25 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     return launch_roster_compact(f, s);
 }
 
-cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)
+// The roots of the deletion's recompute list join the batch's dirty list.
+__global__ void k_mark_dirty(const int* __restrict__ mov, const int* __restrict__ nmov, int* dirty, int* dlist,
+                             int* dcnt)
+{
+    const int n = *nmov;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int r = mov[i];
+        dirty[r] = 1;
+        dlist[atomicAdd(dcnt, 1)] = r;
+    }
+}
+
+__global__ void k_clear_dirty(const int* __restrict__ dlist, const int* __restrict__ dcnt, int* dirty)
+{
+    const int n = *dcnt;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dirty[dlist[i]] = 0;
+}
+
+cudaError_t launch_delete_step(sbc_forest* f, int u, int v, const int* d_removed)
 {
     sbc_graph* g = f->g;
     cudaStream_t s = g->stream;
@@ -264,8 +284,8 @@ cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)
     if ((e = cudaMemsetAsync(f->d_nwork, 0, 2 * sizeof(int), s)) || (e = cudaMemsetAsync(f->d_nmov, 0, 2 * sizeof(int), s)))
         return e;
     k_classify_delete<<<(int)((f->nk * 32 + 255) / 256), 256, 0, s>>>(f->d_dist, f->nv, (int)f->nk, g->dev(), u, v,
-                                                                      d_removed, f->d_worklist, f->d_nwork, f->d_mov,
-                                                                      f->d_nmov, f->d_counters);
+                                                                      d_removed, f->d_dirty, f->d_worklist,
+                                                                      f->d_nwork, f->d_mov, f->d_nmov, f->d_counters);
     if ((e = cudaGetLastError())) return e;
     // roots that keep a parent of the deeper endpoint: incremental
     UpdateArgs A;
@@ -280,31 +300,52 @@ cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)
     A.counters = f->d_counters;
     k_delete<512, 1, 4><<<(int)std::min<int64_t>(f->workers, f->nk), 512, 0, s>>>(A);
     if ((e = cudaGetLastError())) return e;
-    // the others: old dependencies out of BC, recompute, new ones in.  On a
-    // large graph a few roots are recomputed one at a time by the whole GPU
-    // (one CTA would walk the whole graph alone); otherwise the static kernel
-    // recomputes them at once, a CTA per root.
-    int nmov = 0;
-    if ((e = cudaMemcpyAsync(&nmov, f->d_nmov, sizeof(int), cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
-        return e;
-    if (nmov == 0) return cudaSuccess;
+    // the others: their dependencies out of BC now (their state is still that
+    // of the graph before this deletion), recomputed at the end of the batch
     const dim3 grid((unsigned)std::min<int64_t>((f->nv + 255) / 256, 64), (unsigned)std::min<int64_t>(f->nk, 4096));
     k_bc_rows<<<grid, 256, 0, s>>>(f->d_delta, f->d_roots, f->d_mov, f->d_nmov, f->nv, f->d_bc, -1.0);
     if ((e = cudaGetLastError())) return e;
-    if (nmov <= kWideRecompute && f->nv >= kWideRecomputeMinVertices) {
-        std::vector<int> rows(nmov);
-        if ((e = cudaMemcpyAsync(rows.data(), f->d_mov, sizeof(int) * nmov, cudaMemcpyDeviceToHost, s)) ||
+    k_mark_dirty<<<(int)std::min<int64_t>((f->nk + 255) / 256, 64), 256, 0, s>>>(f->d_mov, f->d_nmov, f->d_dirty,
+                                                                                   f->d_dlist, f->d_dcnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_delete_finish(sbc_forest* f)
+{
+    sbc_graph* g = f->g;
+    cudaStream_t s = g->stream;
+    cudaError_t e;
+    int n = 0;
+    if ((e = cudaMemcpyAsync(&n, f->d_dcnt, sizeof(int), cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+        return e;
+    if (n == 0) return cudaSuccess;
+    // a few roots of a large graph: one at a time by the whole GPU (a CTA
+    // would walk the whole graph alone); otherwise a CTA per root
+    if (n <= kWideRecompute && f->nv >= kWideRecomputeMinVertices) {
+        std::vector<int> rows(n);
+        if ((e = cudaMemcpyAsync(rows.data(), f->d_dlist, sizeof(int) * n, cudaMemcpyDeviceToHost, s)) ||
             (e = cudaStreamSynchronize(s)))
             return e;
-        if ((e = recompute_roots_wide(f, rows, f->d_mov))) return e;
-    } else if ((e = launch_static_list(f, f->d_mov, f->d_nmov))) {
+        if ((e = recompute_roots_wide(f, rows, f->d_dlist))) return e;
+    } else if ((e = launch_static_list(f, f->d_dlist, f->d_dcnt))) {
         return e;
     }
-    k_bc_rows<<<grid, 256, 0, s>>>(f->d_delta, f->d_roots, f->d_mov, f->d_nmov, f->nv, f->d_bc, 1.0);
+    const dim3 grid((unsigned)std::min<int64_t>((f->nv + 255) / 256, 64), (unsigned)std::min<int64_t>(f->nk, 4096));
+    k_bc_rows<<<grid, 256, 0, s>>>(f->d_delta, f->d_roots, f->d_dlist, f->d_dcnt, f->nv, f->d_bc, 1.0);
     if ((e = cudaGetLastError())) return e;
-    if ((e = launch_dist2_rows(f, f->d_mov, f->d_nmov))) return e;
-    if ((e = launch_level_hist_list(f, f->d_mov, f->d_nmov))) return e;
-    return launch_roster_build_list(f, f->d_mov, f->d_nmov);
+    if ((e = launch_dist2_rows(f, f->d_dlist, f->d_dcnt))) return e;
+    if ((e = launch_level_hist_list(f, f->d_dlist, f->d_dcnt))) return e;
+    if ((e = launch_roster_build_list(f, f->d_dlist, f->d_dcnt))) return e;
+    k_clear_dirty<<<(int)std::min<int64_t>((f->nk + 255) / 256, 64), 256, 0, s>>>(f->d_dlist, f->d_dcnt, f->d_dirty);
+    if ((e = cudaGetLastError())) return e;
+    return cudaMemsetAsync(f->d_dcnt, 0, sizeof(int), s);
+}
+
+cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)
+{
+    cudaError_t e = launch_delete_step(f, u, v, d_removed);
+    if (e) return e;
+    return launch_delete_finish(f);
 }
 
 }  // namespace sbc

@@ -209,3 +209,56 @@ def test_wide_recompute_on_large_graph(sbc_lib):
         x.close()
     dg.close()
     dg2.close()
+
+
+def test_bridge_deletions_in_one_call(sbc_lib, port_lib):
+    """Deletions in one call: roots whose deeper endpoint loses its last
+    parent leave the call's later deletions to a single recompute on the
+    final graph, while the other roots follow every deletion; chords first
+    keep most roots incremental, tree edges last send many roots to the
+    recompute.
+    The state after the call equals the oracle's, deletion by deletion."""
+    rng = np.random.default_rng(13)
+    n = 400
+    par = np.array([rng.integers(0, i) for i in range(1, n)])
+    tree = np.stack([par, np.arange(1, n)], axis=1)
+    chords = rng.integers(0, n, size=(80, 2))
+    chords = chords[chords[:, 0] != chords[:, 1]]
+    e = np.concatenate([tree, chords])
+    g = G.from_edges(n, np.minimum(e[:, 0], e[:, 1]), np.maximum(e[:, 0], e[:, 1]))
+    roots = G.pick_roots(n, 150, seed=13)
+    edges = _edges(g)
+    # chords first (most roots keep a parent), tree edges last (a bridge cuts
+    # the graph, so every root recomputes from there on)
+    tree_set = set(map(tuple, np.sort(tree, axis=1).tolist()))
+    chord_edges = np.array([e for e in edges.tolist() if tuple(e) not in tree_set], dtype=np.int64)
+    first = chord_edges[rng.choice(len(chord_edges), 20, replace=False)]
+    bridges = np.sort(tree[rng.choice(len(tree), 5, replace=False)], axis=1)
+    taken = set(map(tuple, first.tolist()))
+    bridges = np.array([e for e in bridges.tolist() if tuple(e) not in taken], dtype=np.int64).reshape(-1, 2)
+    dels = np.concatenate([first, bridges])
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    present = [bool(o.delete(int(u), int(v))) for u, v in dels]
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    st = f.delete(dels)
+    assert st["inserted"] == sum(present)
+    assert st["case2"] > 0 and st["case1"] > 0
+    _check(f, o)
+    # and the forest goes on exactly: more deletions and insertions
+    gone = set(map(tuple, dels.tolist()))
+    more = np.asarray([(a, b) for a, b in edges.tolist() if (a, b) not in gone], dtype=np.int64)
+    nxt = more[rng.choice(len(more), 6, replace=False)]
+    for u, v in nxt:
+        o.delete(int(u), int(v))
+    f.delete(nxt)
+    ins = G.uniform_insertions(g, 12, seed=13)
+    ins = np.array([(u, v) for u, v in ins.tolist()], dtype=np.int64)
+    for u, v in ins:
+        o.insert(int(u), int(v))
+    f.insert(ins)
+    _check(f, o)
+    f.close()
+    dg.close()
