@@ -927,9 +927,10 @@ def run_ours(args):
         deletions = {"value": (len(pick) - 1) / del_s, "unit": "deletions/s", "deletions": len(pick) - 1,
                      "removed": dst["inserted"], "incremental_root_pairs": dst["case1"],
                      "recomputed_roots": dst["case2"],
-                     "note": "sbc_delete_batch, host arrays, synchronous: per deletion the edge is removed, roots "
-                             "that keep a parent of the deeper endpoint are updated incrementally, the others "
-                             "recomputed from scratch"}
+                     "note": "sbc_delete_batch, host arrays, synchronous, one call: per deletion the edge is "
+                             "removed and roots that keep a parent of the deeper endpoint are updated incrementally; "
+                             "the others are recomputed from scratch once, on the final graph, after the last "
+                             "deletion"}
 
     cpu = None
     if not args.no_cpu and rank == 0:
