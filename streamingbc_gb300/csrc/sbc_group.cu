@@ -13,6 +13,7 @@
 // members one by one.  Members occupy slots largest first (roots x vertices),
 // which puts the longest items at the front of the queue.
 #include <algorithm>
+#include <vector>
 #include "sbc_host.h"
 #include "sbc_update_job.cuh"
 
@@ -149,15 +150,20 @@ cudaError_t launch_group_update(sbc_group* G, const int* counts, unsigned steps)
         const int grid = (int)std::min<int64_t>(G->ws.workers, total);
         kGroupVariants[G->variant].launch(A, grid, s);
         if ((e = cudaGetLastError())) return e;
-        for (int i = 0; i < ns; ++i)
-            if ((e = launch_roster_compact(G->members[i], s))) return e;
+        if ((e = launch_roster_compact_forests(G->members.data(), ns, s))) return e;
     }
     if (steps & GROUP_SEAL) {
         if ((e = launch_seal_group(B, s))) return e;
         // level-2 masks of every forest on the members' graphs
+        std::vector<sbc_forest*> fs;
+        std::vector<int> fc;
         for (int i = 0; i < ns; ++i)
-            for (sbc_forest* f : G->members[i]->g->forests)
-                if ((e = launch_l2mask_insert_forest(f, counts[i], false, s))) return e;
+            for (sbc_forest* f : G->members[i]->g->forests) {
+                if (std::find(fs.begin(), fs.end(), f) != fs.end()) continue;
+                fs.push_back(f);
+                fc.push_back(counts[i]);
+            }
+        if ((e = launch_l2mask_insert_forests(fs.data(), fc.data(), (int)fs.size(), false, s))) return e;
     }
     return cudaSuccess;
 }

@@ -432,6 +432,10 @@ cudaError_t launch_l2mask_build_all(sbc_forest* f);
 // *d_removed (directed: the u -> v slot only).
 cudaError_t launch_l2mask_insert(sbc_graph* g, int n, bool directed);
 cudaError_t launch_l2mask_insert_forest(sbc_forest* f, int n, bool directed, cudaStream_t s);
+// The same for nf forests (counts[j] insertions staged on fs[j]'s graph), one
+// launch per step for up to kMaxGroup forests.
+cudaError_t launch_l2mask_insert_forests(sbc_forest* const* fs, const int* counts, int nf, bool directed,
+                                        cudaStream_t s);
 cudaError_t launch_l2mask_remove(sbc_graph* g, int u, int v, bool directed, const int* d_removed);
 cudaError_t launch_roster_build_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 // Cost model and schedule (sbc_model.cu).
@@ -440,6 +444,7 @@ cudaError_t launch_level_hist(sbc_forest* f);
 // compaction of rosters that hold stale entries (after each batch).
 cudaError_t launch_roster_build(sbc_forest* f);
 cudaError_t launch_roster_compact(sbc_forest* f, cudaStream_t s);
+cudaError_t launch_roster_compact_forests(sbc_forest* const* fs, int nf, cudaStream_t s);
 // Before the update of a batch of n: features of every active (root,
 // insertion) pair into the log buffers (when logging) and, under the model
 // schedule, the worklist ordered by predicted cost (longest first);

@@ -16,8 +16,10 @@
 //                    mask[r][x]; an edge at the root flags the root.
 //   k_l2mask_remove  after an edge removal (thread per root): clears the bits
 //                    of the removed slots; an edge at the root flags it.
+//   *_group          the same for several forests in one launch per step.
 // Masks describe the edges that existed when a batch began; the update adds
 // the edges its batch appended before the job (visible by seq) itself.
+#include <algorithm>
 #include "sbc_host.h"
 #include "sbc_internal.cuh"
 
@@ -75,16 +77,11 @@ __global__ void __launch_bounds__(512) k_l2mask_build(DevGraph G, const int64_t*
     }
 }
 
-__global__ void k_l2mask_insert(const int64_t* __restrict__ roots, int nk, int n, const int32_t* __restrict__ iu,
-                                const int32_t* __restrict__ iv, const int32_t* __restrict__ ok, int directed,
-                                int64_t nv, uint32_t* mask, const int32_t* __restrict__ cand,
-                                const int32_t* __restrict__ l1n, int32_t* flag, int32_t* list, int32_t* cnt)
+// The masks of root r after the append of insertion (u, v).
+__device__ __forceinline__ void insert_one(const int64_t* roots, int r, int u, int v, int directed, int64_t nv,
+                                           uint32_t* mask, const int32_t* cand, const int32_t* l1n, int32_t* flag,
+                                           int32_t* list, int32_t* cnt)
 {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= (int64_t)nk * n) return;
-    const int r = (int)(t / n), i = (int)(t % n);
-    if (ok[i] <= 0) return;
-    const int u = iu[i], v = iv[i];
     const int root = (int)roots[r];
     if (u == root || v == root) {
         flag_rebuild(flag, list, cnt, r);
@@ -100,6 +97,81 @@ __global__ void k_l2mask_insert(const int64_t* __restrict__ roots, int nk, int n
         const int bu = l1_index(C, c, u);  // slot v -> u
         if (bu >= 0) atomicOr(&M[v], 1u << bu);
     }
+}
+
+__global__ void k_l2mask_insert(const int64_t* __restrict__ roots, int nk, int n, const int32_t* __restrict__ iu,
+                                const int32_t* __restrict__ iv, const int32_t* __restrict__ ok, int directed,
+                                int64_t nv, uint32_t* mask, const int32_t* __restrict__ cand,
+                                const int32_t* __restrict__ l1n, int32_t* flag, int32_t* list, int32_t* cnt)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nk * n) return;
+    const int r = (int)(t / n), i = (int)(t % n);
+    if (ok[i] <= 0) return;
+    insert_one(roots, r, iu[i], iv[i], directed, nv, mask, cand, l1n, flag, list, cnt);
+}
+
+// Several forests in one launch per step (the forests on the graphs of a
+// group batch): one entry per forest with its staged insertions.
+struct MaskForest {
+    DevGraph G;
+    const int64_t* roots;
+    uint32_t* mask;
+    int32_t* cand;
+    int32_t* l1n;
+    int32_t* flag;
+    int32_t* list;
+    int32_t* cnt;
+    const int32_t* iu;
+    const int32_t* iv;
+    const int32_t* ok;
+    int nk;
+    int n;
+};
+
+struct MaskGroupArgs {
+    MaskForest f[kMaxGroup];
+    int64_t base[kMaxGroup + 1];  // prefix sums of nk * n
+    int nf;
+    int directed;
+};
+
+// One thread per (forest, root, insertion).
+__global__ void k_l2mask_insert_group(const __grid_constant__ MaskGroupArgs A)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= A.base[A.nf]) return;
+    int lo = 0, hi = A.nf - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.base[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const MaskForest& F = A.f[lo];
+    const int64_t local = t - A.base[lo];
+    const int r = (int)(local / F.n), i = (int)(local % F.n);
+    if (F.ok[i] <= 0) return;
+    insert_one(F.roots, r, F.iu[i], F.iv[i], A.directed, F.G.nv, F.mask, F.cand, F.l1n, F.flag, F.list, F.cnt);
+}
+
+// The flagged roots of every forest, CTA per root.
+__global__ void __launch_bounds__(512) k_l2mask_build_group(const __grid_constant__ MaskGroupArgs A)
+{
+    for (int j = 0; j < A.nf; ++j) {
+        const MaskForest& F = A.f[j];
+        const int n = *F.cnt;
+        for (int item = blockIdx.x; item < n; item += gridDim.x) {
+            const int r = F.list[item];
+            build_root(F.G, F.roots, F.mask, F.cand, F.l1n, r);
+            if (threadIdx.x == 0) F.flag[r] = 0;
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void k_l2mask_reset_group(const __grid_constant__ MaskGroupArgs A)
+{
+    if ((int)threadIdx.x < A.nf) *A.f[threadIdx.x].cnt = 0;
 }
 
 __global__ void k_l2mask_remove(const int64_t* __restrict__ roots, int nk, int u, int v, int directed,
@@ -160,6 +232,48 @@ cudaError_t launch_l2mask_insert_forest(sbc_forest* f, int n, bool directed, cud
     cudaError_t e = cudaGetLastError();
     if (e) return e;
     return rebuild_flagged(f, s);
+}
+
+cudaError_t launch_l2mask_insert_forests(sbc_forest* const* fs, const int* counts, int nf, bool directed,
+                                        cudaStream_t s)
+{
+    for (int at = 0; at < nf; at += kMaxGroup) {
+        MaskGroupArgs A;
+        A.nf = 0;
+        A.directed = directed ? 1 : 0;
+        A.base[0] = 0;
+        for (int j = at; j < std::min(nf, at + kMaxGroup); ++j) {
+            sbc_forest* f = fs[j];
+            if (!f->d_l2mask || counts[j] <= 0) continue;
+            sbc_graph* g = f->g;
+            MaskForest& F = A.f[A.nf];
+            F.G = g->dev();
+            F.roots = f->d_roots;
+            F.mask = f->d_l2mask;
+            F.cand = f->d_l1cand;
+            F.l1n = f->d_l1n;
+            F.flag = f->d_l2flag;
+            F.list = f->d_l2list;
+            F.cnt = f->d_l2cnt;
+            F.iu = g->d_ins;
+            F.iv = g->d_ins + g->ins_capacity;
+            F.ok = g->d_ins + 2 * g->ins_capacity;
+            F.nk = (int)f->nk;
+            F.n = counts[j];
+            A.base[A.nf + 1] = A.base[A.nf] + f->nk * (int64_t)counts[j];
+            ++A.nf;
+        }
+        if (A.nf == 0) continue;
+        const int64_t threads = A.base[A.nf];
+        k_l2mask_insert_group<<<(int)((threads + 255) / 256), 256, 0, s>>>(A);
+        cudaError_t e = cudaGetLastError();
+        if (e) return e;
+        k_l2mask_build_group<<<64, 512, 0, s>>>(A);
+        if ((e = cudaGetLastError())) return e;
+        k_l2mask_reset_group<<<1, kMaxGroup, 0, s>>>(A);
+        if ((e = cudaGetLastError())) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_l2mask_insert(sbc_graph* g, int n, bool directed)

@@ -17,7 +17,8 @@
 // k_roster_compact drops stale entries after each batch.
 //   k_roster_build    CTA per root: members of levels 2..kRosterLevels-1 whose
 //                     level histogram count fits a roster (after static init)
-//   k_roster_compact  warp per (root, level) roster marked stale
+//   k_roster_compact  warp per (root, level) roster marked stale (the _group
+//                     form: for several forests in one launch)
 #include "sbc_host.h"
 #include "sbc_internal.cuh"
 
@@ -55,13 +56,11 @@ __global__ void __launch_bounds__(256) k_roster_build(const uint8_t* __restrict_
     }
 }
 
-__global__ void __launch_bounds__(256) k_roster_compact(const uint8_t* __restrict__ dist8, int64_t nv, int nk,
-                                                        int32_t* __restrict__ roster, int32_t* __restrict__ roster_n,
-                                                        int32_t* __restrict__ dirty)
+// Warp w = root * kRosterLevels + level drops the stale entries of its roster.
+__device__ __forceinline__ void compact_one(const uint8_t* __restrict__ dist8, int64_t nv,
+                                            int32_t* __restrict__ roster, int32_t* __restrict__ roster_n,
+                                            int32_t* __restrict__ dirty, int w, int lane)
 {
-    const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (w >= nk * kRosterLevels) return;
     if (!dirty[w]) return;  // warp-uniform
     const int n = roster_n[w];
     if (n > kRosterCap) return;
@@ -83,6 +82,70 @@ __global__ void __launch_bounds__(256) k_roster_compact(const uint8_t* __restric
         roster_n[w] = kept;
         dirty[w] = 0;
     }
+}
+
+__global__ void __launch_bounds__(256) k_roster_compact(const uint8_t* __restrict__ dist8, int64_t nv, int nk,
+                                                        int32_t* __restrict__ roster, int32_t* __restrict__ roster_n,
+                                                        int32_t* __restrict__ dirty)
+{
+    const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    if (w >= nk * kRosterLevels) return;
+    compact_one(dist8, nv, roster, roster_n, dirty, w, threadIdx.x & 31);
+}
+
+// Several forests in one launch (the members of a group batch).
+struct RosterForest {
+    const uint8_t* dist8;
+    int64_t nv;
+    int32_t* roster;
+    int32_t* roster_n;
+    int32_t* dirty;
+};
+
+struct RosterGroupArgs {
+    RosterForest f[kMaxGroup];
+    int64_t wbase[kMaxGroup + 1];  // prefix sums of nk * kRosterLevels
+    int nf;
+};
+
+__global__ void __launch_bounds__(256) k_roster_compact_group(const __grid_constant__ RosterGroupArgs A)
+{
+    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (w >= A.wbase[A.nf]) return;
+    int lo = 0, hi = A.nf - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.wbase[mid] <= w) lo = mid;
+        else hi = mid - 1;
+    }
+    const RosterForest& F = A.f[lo];
+    compact_one(F.dist8, F.nv, F.roster, F.roster_n, F.dirty, (int)(w - A.wbase[lo]), threadIdx.x & 31);
+}
+
+cudaError_t launch_roster_compact_forests(sbc_forest* const* fs, int nf, cudaStream_t s)
+{
+    for (int at = 0; at < nf; at += kMaxGroup) {
+        RosterGroupArgs A;
+        A.nf = 0;
+        A.wbase[0] = 0;
+        for (int j = at; j < nf && j < at + kMaxGroup; ++j) {
+            sbc_forest* f = fs[j];
+            if (!f->d_roster) continue;
+            RosterForest& F = A.f[A.nf];
+            F.dist8 = f->d_dist8;
+            F.nv = f->nv;
+            F.roster = f->d_roster;
+            F.roster_n = f->d_roster_n;
+            F.dirty = f->d_roster_dirty;
+            A.wbase[A.nf + 1] = A.wbase[A.nf] + f->nk * kRosterLevels;
+            ++A.nf;
+        }
+        if (A.nf == 0) continue;
+        k_roster_compact_group<<<(int)((A.wbase[A.nf] * 32 + 255) / 256), 256, 0, s>>>(A);
+        cudaError_t e = cudaGetLastError();
+        if (e) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_roster_build(sbc_forest* f) { return launch_roster_build_list(f, nullptr, nullptr); }

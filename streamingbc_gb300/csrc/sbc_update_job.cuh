@@ -379,11 +379,15 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 const int qbase = sm.st;  // free tail of the same-level queue holds the two lists
                 for (int i = threadIdx.x; i < nn1 + nn2; i += NT) {
                     const int x = i < nn1 ? nl1[i] : nl2[i - nn1];
+                    // loads that need only x, issued before commit's stores
+                    const int64_t rx = A.G.row[x];
+                    const int xd0 = A.G.deg0[x], xd = A.G.deg[x];
+                    const unsigned m0 = (L == 2 && M2) ? M2[x] : 0u;
                     double wn, wd;
                     commit(x, wn, wd);
                     W.acc[x] = wn;
                     W.dp[x] = (int64_t)__double_as_longlong(wd);
-                    const int dx = vis_deg(A.G, x, A.G.row[x], g);
+                    const int dx = (xd0 == xd || g == INT_MAX) ? xd : vis_deg(A.G, x, rx, g);
                     push_cost += dx;
                     if (L == 1) {
                         root_sum += (rootDown || (root == a && x == b)) ? wn : wd;
@@ -391,9 +395,8 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                         // parents from the mask (edges older than the batch),
                         // plus this batch's edges visible here that reach a root
                         // neighbour (level 1)
-                        unsigned m = M2[x];
-                        const int64_t rx = A.G.row[x];
-                        for (int sl = A.G.deg0[x]; sl < dx; ++sl) {
+                        unsigned m = m0;
+                        for (int sl = xd0; sl < dx; ++sl) {
                             const int z = A.G.col[rx + sl];
                             if (D8[z] == 1)
                                 for (int q = 0; q < n1; ++q)
