@@ -925,12 +925,14 @@ def run_ours(args):
         dst = f.delete(pick[1:])
         del_s = time.perf_counter() - t1
         deletions = {"value": (len(pick) - 1) / del_s, "unit": "deletions/s", "deletions": len(pick) - 1,
-                     "removed": dst["inserted"], "incremental_root_pairs": dst["case1"],
-                     "recomputed_roots": dst["case2"],
-                     "note": "sbc_delete_batch, host arrays, synchronous, one call: per deletion the edge is "
-                             "removed and roots that keep a parent of the deeper endpoint are updated incrementally; "
-                             "the others are recomputed from scratch once, on the final graph, after the last "
-                             "deletion"}
+                     "removed": dst["inserted"], "keep_parent_pairs": dst["case1"],
+                     "lost_parent_pairs": dst["case2"],
+                     "note": "sbc_delete_batch, host arrays, synchronous, one call and one update launch: removals "
+                             "marked in order, every affected root runs the deletions in order (each job sees the "
+                             "graph after its deletion): sigma-only update where the deeper endpoint keeps a parent, "
+                             "else the affected vertices move down in place (graphs of >= 32768 vertices) or the "
+                             "root is recomputed once on the final graph (smaller graphs, or a move-down over "
+                             "max(1024, V/16) vertices)"}
 
     cpu = None
     if not args.no_cpu and rank == 0:

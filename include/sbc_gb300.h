@@ -353,15 +353,28 @@ int sbc_server_get_stats(sbc_server *s, sbc_server_stats *stats, int reset);
  * endpoints on one level (or both unreachable) change nothing; otherwise the
  * deeper endpoint b either keeps a parent -- sigma-only decrease and
  * dependency ascent, the reference's removeEdgeWithoutMovementBrandes
- * (src/streamingbc_internal.c:607-868) -- or loses its last one, and the root
- * is recomputed from scratch (BC moved by its new minus old dependencies)
- * instead of the reference's moveDownTreeBrandes (:880-1401), whose results
- * disagree with a recomputation of the modified graph.  Results equal a
- * static recompute of the modified graph (tested).  stats->inserted counts
- * edges removed, duplicates edges absent, invalid bad ids; case1/case2 the
- * incremental / recomputed (root, deletion) pairs. */
-/* Remove n undirected edges from the graph one at a time, each followed by
- * the update of every root.  Synchronous; stats may be NULL. */
+ * (src/streamingbc_internal.c:607-868) -- or loses its last one, the
+ * reference's moveDownTreeBrandes (:880-1401), whose results disagree with a
+ * recomputation of the modified graph.  Here that case either moves the
+ * affected vertices down in place (exact: new levels, sigma and dependencies
+ * of the changed part only) or recomputes the root from scratch once, after
+ * the call's last deletion (BC moved by its new minus old dependencies; the
+ * root skips the call's later deletions).  SBC_DELETE_AUTO moves down on
+ * graphs of >= 32768 vertices and recomputes on smaller ones, where a whole
+ * recompute is cheap; a move-down whose affected set exceeds max(1024, V/16)
+ * vertices falls back to the recompute.  Results equal a static recompute of
+ * the modified graph in every mode (tested).  stats->inserted counts edges
+ * removed, duplicates edges absent, invalid bad ids; case1/case2 the
+ * (root, deletion) pairs whose deeper endpoint keeps / loses its parents. */
+#define SBC_DELETE_AUTO 0
+#define SBC_DELETE_MOVE_DOWN 1
+#define SBC_DELETE_RECOMPUTE 2
+int sbc_forest_set_delete_mode(sbc_forest *f, int mode);
+/* Remove n undirected edges in order, with the update of every root after
+ * each, as n single deletions would.  One update launch serves the whole
+ * call: the removed slots stay marked in place until it ends, so each
+ * deletion's jobs see the graph without the edges of that deletion and the
+ * earlier ones.  Synchronous; stats may be NULL. */
 int sbc_delete_batch(sbc_forest *f, int64_t n, const int64_t *u, const int64_t *v, sbc_batch_stats *stats);
 /* The update for one deletion whose edge the caller has already removed in
  * both directions (sbc_graph_remove_directed x2, or stinger_remove_edge x2),

@@ -1042,6 +1042,14 @@ int sbc_forest_set_variant(sbc_forest* f, int variant)
     return SBC_OK;
 }
 
+int sbc_forest_set_delete_mode(sbc_forest* f, int mode)
+{
+    if (!f || mode < SBC_DELETE_AUTO || mode > SBC_DELETE_RECOMPUTE)
+        return fail(SBC_ERR_ARG, "sbc_forest_set_delete_mode: bad arguments");
+    f->delete_mode = mode;
+    return SBC_OK;
+}
+
 int sbc_forest_variant(const sbc_forest* f, int* variant)
 {
     if (!f || !variant) return fail(SBC_ERR_ARG, "sbc_forest_variant: null");
@@ -1218,19 +1226,17 @@ int sbc_delete_batch(sbc_forest* f, int64_t n, const int64_t* u, const int64_t* 
         if (stats) memset(stats, 0, sizeof *stats);
         return SBC_OK;
     }
-    int rc = ensure_staging(g, n);
+    int rc = stage_host(g, n, u, v, false);
     if (rc) return rc;
-    int32_t* codes = g->d_ins + 2 * g->ins_capacity;
+    const int32_t* codes = g->d_ins + 2 * g->ins_capacity;
     if (stats) CK(cudaMemsetAsync(f->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, g->stream));
-    // one deletion at a time, in order: remove the edge, then update every
-    // root that keeps a parent of the deeper endpoint; roots that lose it are
-    // recomputed once, on the final graph, after the last deletion
-    for (int64_t i = 0; i < n; ++i) {
-        const bool valid = u[i] >= 0 && v[i] >= 0 && u[i] < g->nv && v[i] < g->nv && u[i] != v[i];
-        const int a = valid ? (int)u[i] : -1, b = valid ? (int)v[i] : -1;
-        CK(sbc::launch_remove(g, a, b, false, codes + i));
-        if (valid) CK(sbc::launch_delete_step(f, a, b, codes + i));
-    }
+    // the whole batch in one update launch: removals marked in order, every
+    // root through the deletions in order (each job seeing the graph as it
+    // stands after its deletion), the marked slots compacted, and the roots
+    // left to a recompute recomputed once, on the final graph
+    CK(sbc::launch_mark_removed(g, (int)n));
+    CK(sbc::launch_delete_batch(f, (int)n));
+    CK(sbc::launch_compact_removed(g, (int)n));
     CK(sbc::launch_delete_finish(f));
     if (stats) return deletion_stats(f, n, codes, stats);
     CK(cudaStreamSynchronize(g->stream));

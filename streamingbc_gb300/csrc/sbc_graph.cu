@@ -293,6 +293,100 @@ __global__ void k_remove(int64_t nv, const int64_t* __restrict__ row, int32_t* d
     if (threadIdx.x == 0) *res = code;
 }
 
+// Batched deletions, step 1: the n staged edges (iu/iv, -1 = invalid id) are
+// removed in order, each only marked -- its two slots keep their place and get
+// seq = -1 - i -- so that every deletion's update can still see the graph as
+// it stood before it (a slot removed at deletion j is an edge for jobs i < j).
+// code[i] = 1 removed, 0 absent (never there, or removed earlier in the
+// batch), -1 self loop / bad id.  One thread: each lookup is a binary search
+// of the sorted leading slots, then a scan of any unsorted tail.
+__device__ __forceinline__ int64_t live_slot(const int64_t* row, const int32_t* deg, const int32_t* nsort,
+                                             const int32_t* col, const int32_t* seq, int x, int y)
+{
+    const int64_t rx = row[x];
+    const int d = deg[x], ns = min(nsort[x], d);
+    int lo = 0, hi = ns;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const int c = col[rx + mid];
+        if (c < y) lo = mid + 1;
+        else if (c > y) hi = mid;
+        else return seq[rx + mid] >= 0 ? rx + mid : -1;
+    }
+    for (int s2 = ns; s2 < d; ++s2)
+        if (col[rx + s2] == y && seq[rx + s2] >= 0) return rx + s2;
+    return -1;
+}
+
+__global__ void k_mark_removed(const int64_t* __restrict__ row, const int32_t* __restrict__ deg,
+                               const int32_t* __restrict__ nsort, const int32_t* __restrict__ col, int32_t* seq, int n,
+                               const int32_t* __restrict__ iu, const int32_t* __restrict__ iv, int32_t* code)
+{
+    if (threadIdx.x != 0) return;
+    for (int i = 0; i < n; ++i) {
+        const int u = iu[i], v = iv[i];
+        if (u < 0 || v < 0 || u == v) {
+            code[i] = -1;
+            continue;
+        }
+        const int64_t pu = live_slot(row, deg, nsort, col, seq, u, v);
+        const int64_t pv = pu < 0 ? -1 : live_slot(row, deg, nsort, col, seq, v, u);
+        if (pu < 0 || pv < 0) {
+            code[i] = 0;
+            continue;
+        }
+        seq[pu] = -1 - i;
+        seq[pv] = -1 - i;
+        code[i] = 1;
+    }
+}
+
+// Batched deletions, step 3 (after the update): the marked slots leave their
+// lists, which keep their order.  CTA per deletion endpoint; an endpoint that
+// an earlier removed deletion also names is left to that deletion's CTA.
+__global__ void __launch_bounds__(256) k_compact_removed(const int64_t* __restrict__ row, int32_t* deg, int32_t* deg0,
+                                                         int32_t* nsort, int32_t* col, int32_t* seq, int n,
+                                                         const int32_t* __restrict__ iu,
+                                                         const int32_t* __restrict__ iv,
+                                                         const int32_t* __restrict__ code)
+{
+    __shared__ int s_warp[8];
+    __shared__ int s_keep_sorted;
+    const int i = blockIdx.x >> 1;
+    if (code[i] != 1) return;
+    const int x = (blockIdx.x & 1) ? iv[i] : iu[i];
+    for (int j = 0; j < i; ++j)
+        if (code[j] == 1 && (iu[j] == x || iv[j] == x)) return;
+    const int64_t rx = row[x];
+    const int d = deg[x], ns = min(nsort[x], d);
+    if (threadIdx.x == 0) s_keep_sorted = 0;
+    int kept = 0;
+    for (int base = 0; base < d; base += 256) {
+        const int sl = base + (int)threadIdx.x;
+        int c = 0, q = 0;
+        bool keep = false;
+        if (sl < d) {
+            c = col[rx + sl];
+            q = seq[rx + sl];
+            keep = q >= 0;
+        }
+        int total;
+        const int off = block_exclusive_scan<256>(keep ? 1 : 0, s_warp, &total);  // every read precedes its barrier
+        if (keep) {
+            col[rx + kept + off] = c;
+            seq[rx + kept + off] = q;
+        }
+        if (keep && sl < ns) atomicAdd(&s_keep_sorted, 1);
+        kept += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        deg[x] = kept;
+        deg0[x] = kept;
+        nsort[x] = s_keep_sorted;
+    }
+}
+
 // k_seal over many graphs: blockIdx.y selects the graph.
 __global__ void k_seal_group(const __grid_constant__ GraphBatchSlots S)
 {
@@ -388,6 +482,24 @@ cudaError_t launch_remove(sbc_graph* g, int u, int v, bool directed, int* d_res)
     cudaError_t e = cudaGetLastError();
     if (e) return e;
     return launch_l2mask_remove(g, u, v, directed, d_res);
+}
+
+cudaError_t launch_mark_removed(sbc_graph* g, int n)
+{
+    k_mark_removed<<<1, 32, 0, g->stream>>>(g->d_row, g->d_deg, g->d_nsort, g->d_col, g->d_seq, n, g->d_ins,
+                                           g->d_ins + g->ins_capacity, g->d_ins + 2 * g->ins_capacity);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact_removed(sbc_graph* g, int n)
+{
+    if (n <= 0) return cudaSuccess;
+    k_compact_removed<<<2 * n, 256, 0, g->stream>>>(g->d_row, g->d_deg, g->d_deg0, g->d_nsort, g->d_col, g->d_seq, n,
+                                                    g->d_ins, g->d_ins + g->ins_capacity,
+                                                    g->d_ins + 2 * g->ins_capacity);
+    cudaError_t e = cudaGetLastError();
+    if (e) return e;
+    return launch_l2mask_remove_batch(g, n);
 }
 
 cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new_col, int32_t* d_new_seq)

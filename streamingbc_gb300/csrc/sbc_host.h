@@ -178,6 +178,7 @@ struct sbc_forest {
     // persistent workers and their scratch
     int sm_count = 0;
     int variant = 0;  // launch shape of the update kernel
+    int delete_mode = 0;  // SBC_DELETE_*: lost-parent roots moved down or recomputed
     int64_t workers = 0;      // == ws.workers
     int64_t workers_req = 0;  // worker count the caller asked for (0 = one per resident CTA)
     int groups = 0;           // groups this forest is a member of
@@ -200,7 +201,7 @@ struct sbc_forest {
     int64_t state_bytes = 0;
     WorkerScratch ws;
     int* d_worklist = nullptr;
-    int* d_mov = nullptr;     // [nk] roots a deletion leaves without a parent of the deeper endpoint
+    int* d_mov = nullptr;     // [nk] roots of a deletion left to a recompute (move-down over its cap)
     int* d_nmov = nullptr;    // [2]: their count, work counter
     // roots left for a recompute at the end of a deletion batch: [nk] flags,
     // [nk] list, [1] count
@@ -402,15 +403,18 @@ cudaError_t launch_repack(sbc_graph* g, const int64_t* d_new_row, int32_t* d_new
 cudaError_t launch_remove(sbc_graph* g, int u, int v, bool directed, int* d_res);
 // Update for the deletion of (u, v), already removed from the adjacency
 // (*d_removed must be 1, else nothing is done): roots that keep a parent of the
-// deeper endpoint get the sigma-decrease descent and ascent; the others are
-// recomputed from scratch, their old dependencies taken out of BC first.
-// One deletion of a batch (edge already removed when *d_removed == 1): roots
-// that keep a parent of the deeper endpoint are updated, the others take
-// their BC row out and are left for launch_delete_finish, which recomputes
-// them once on the batch's final graph and puts their rows back.
+// deeper endpoint get the sigma-decrease descent and ascent; the others move
+// down or are recomputed from scratch (SBC_DELETE_*), a recomputed root's old
+// dependencies taken out of BC first.
+// launch_delete_step: the update of one deletion, recomputes left for
+// launch_delete_finish, which recomputes the listed roots once on the graph as
+// it then stands and puts their rows back.
 cudaError_t launch_delete_step(sbc_forest* f, int u, int v, const int* d_removed);
 cudaError_t launch_delete_finish(sbc_forest* f);
 cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed);
+// Every root through the n deletions marked in g's staging (launch_mark_removed),
+// in one persistent launch; dirty roots are left for launch_delete_finish.
+cudaError_t launch_delete_batch(sbc_forest* f, int n);
 // Static recompute of the roots listed (device list and count) or, with a
 // null list, of all roots.
 cudaError_t launch_static_list(sbc_forest* f, const int* d_list, const int* d_nlist);
@@ -437,6 +441,14 @@ cudaError_t launch_l2mask_insert_forest(sbc_forest* f, int n, bool directed, cud
 cudaError_t launch_l2mask_insert_forests(sbc_forest* const* fs, const int* counts, int nf, bool directed,
                                         cudaStream_t s);
 cudaError_t launch_l2mask_remove(sbc_graph* g, int u, int v, bool directed, const int* d_removed);
+// ... and after the n removals staged in g (undirected; codes in the staging's
+// third row), once their slots are compacted.
+cudaError_t launch_l2mask_remove_batch(sbc_graph* g, int n);
+// Batched deletions of the n edges staged in g: removal marks in order
+// (codes into the staging's third row), and after the update the compaction
+// of the marked slots (and the masks' upkeep).
+cudaError_t launch_mark_removed(sbc_graph* g, int n);
+cudaError_t launch_compact_removed(sbc_graph* g, int n);
 cudaError_t launch_roster_build_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 // Cost model and schedule (sbc_model.cu).
 cudaError_t launch_level_hist(sbc_forest* f);
@@ -445,6 +457,9 @@ cudaError_t launch_level_hist(sbc_forest* f);
 cudaError_t launch_roster_build(sbc_forest* f);
 cudaError_t launch_roster_compact(sbc_forest* f, cudaStream_t s);
 cudaError_t launch_roster_compact_forests(sbc_forest* const* fs, int nf, cudaStream_t s);
+// Deletions move lost-parent roots down (rather than recompute them) on graphs
+// of at least this many vertices under SBC_DELETE_AUTO.
+constexpr int64_t kMoveDownMinVertices = 32768;
 // Before the update of a batch of n: features of every active (root,
 // insertion) pair into the log buffers (when logging) and, under the model
 // schedule, the worklist ordered by predicted cost (longest first);

@@ -55,6 +55,19 @@ struct DevGraph {
     const int32_t* seq;
 };
 
+// Whether slot p is still an edge for the job with sequence g.  TOMB: a batch
+// of deletions is under way, whose removed slots stay in place until it ends
+// with seq = -1 - i (i = the deletion that removed them), so the job of
+// deletion g skips those removed at deletions <= g.  Every other walker is
+// compiled without the test.
+template <bool TOMB>
+__device__ __forceinline__ bool slot_live(const DevGraph& G, int64_t p, int g)
+{
+    if (!TOMB) return true;
+    const int q = G.seq[p];
+    return q >= 0 || -1 - q > g;
+}
+
 // One forest as an update launch sees it: its graph, its root-major state and
 // the insertion batch staged for it (endpoints and append codes).
 struct ForestSlot {
@@ -165,7 +178,8 @@ __device__ __forceinline__ int vis_deg(const DevGraph& G, int x, int64_t rs, int
 // Is y among the first vx (visible) neighbours of x, whose slots start at rx?
 // Binary search of the sorted leading slots, then a scan of the appended tail.
 // Adds the number of slots examined to *cost.
-__device__ __forceinline__ bool has_edge(const DevGraph& G, int x, int64_t rx, int vx, int y, unsigned& cost)
+template <bool TOMB = false>
+__device__ __forceinline__ bool has_edge(const DevGraph& G, int x, int64_t rx, int vx, int y, int g, unsigned& cost)
 {
     const int ns = min(G.nsort[x], vx);
     int lo = 0, hi = ns;
@@ -175,11 +189,11 @@ __device__ __forceinline__ bool has_edge(const DevGraph& G, int x, int64_t rx, i
         ++cost;
         if (c < y) lo = mid + 1;
         else if (c > y) hi = mid;
-        else return true;
+        else return slot_live<TOMB>(G, rx + mid, g);
     }
     for (int s = ns; s < vx; ++s) {
         ++cost;
-        if (G.col[rx + s] == y) return true;
+        if (G.col[rx + s] == y) return slot_live<TOMB>(G, rx + s, g);
     }
     return false;
 }
@@ -310,9 +324,9 @@ constexpr int kEdgeIlp = 4;
 // most NT edges still gives every thread one edge and no thread a serial chain
 // of several.  Sets kk[u] (neighbour, -1 past the end) and jj[u] (chunk vertex)
 // for u < per; j is the thread's current chunk vertex, which only moves forward.
-template <int NT, int ILP>
+template <int NT, int ILP, bool TOMB>
 __device__ __forceinline__ void walk_fetch(const DevGraph& G, const LbSmem<NT>& sm, int cnt, int total, int e0,
-                                           int per, int& j, int (&kk)[ILP], int (&jj)[ILP])
+                                           int per, int g, int& j, int (&kk)[ILP], int (&jj)[ILP])
 {
 #pragma unroll
     for (int u = 0; u < ILP; ++u) {
@@ -333,7 +347,9 @@ __device__ __forceinline__ void walk_fetch(const DevGraph& G, const LbSmem<NT>& 
                 j = lo;
             }
             jj[u] = j;
-            kk[u] = G.col[sm.row[j] + (e - sm.off[j])];
+            const int64_t p = sm.row[j] + (e - sm.off[j]);
+            kk[u] = G.col[p];
+            if (!slot_live<TOMB>(G, p, g)) kk[u] = -1;
         }
     }
 }
@@ -370,7 +386,7 @@ __device__ __forceinline__ void gather_dist(const DistRow& dr, const int (&kk)[I
 // >= 254).  post(j, x) runs after the chunk's edges.  Ends with a barrier.
 // REF: the walked vertices and their degrees count as traversed in the
 // reference's sense (COUNT_TRAVERSALS); every walk counts its scanned slots.
-template <int NT, bool REF = true, int ILP = kEdgeIlp, class Prep, class Edge, class Post>
+template <int NT, bool REF = true, int ILP = kEdgeIlp, bool TOMB = false, class Prep, class Edge, class Post>
 __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const DistRow dr,
                                         const int32_t* l1, int n1, const int32_t* l2, int n2, LbSmem<NT>& sm,
                                         Prep prep, Edge edge, Post post)
@@ -405,7 +421,7 @@ __device__ __forceinline__ void lb_walk(const DevGraph& G, int g, const DistRow 
         const int per = min(ILP, (total + NT - 1) / NT);
         for (int e0 = t * per; e0 < total; e0 += NT * per) {
             int kk[ILP], jj[ILP], dk[ILP];
-            walk_fetch<NT, ILP>(G, sm, cnt, total, e0, per, j, kk, jj);
+            walk_fetch<NT, ILP, TOMB>(G, sm, cnt, total, e0, per, g, j, kk, jj);
             gather_dist<ILP>(dr, kk, dk);
 #pragma unroll
             for (int u = 0; u < ILP; ++u)
@@ -433,7 +449,7 @@ struct NoPost {
 // GATHER = false skips the distance gather (contrib then receives 0), for
 // walks whose edge test needs no distance.
 constexpr int kSumHit = 4;
-template <int NT, bool GATHER, int ILP = kEdgeIlp, class Prep, class Contrib, class Post>
+template <int NT, bool GATHER, int ILP = kEdgeIlp, bool TOMB = false, class Prep, class Contrib, class Post>
 __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const DistRow dr,
                                             const int32_t* l1, int n1, LbSmem<NT>& sm, double* s_sum, int* s_hit,
                                             Prep prep, Contrib contrib, Post post)
@@ -465,7 +481,7 @@ __device__ __forceinline__ void lb_walk_sum(const DevGraph& G, int g, const Dist
         const int per = min(ILP, (total + NT - 1) / NT);
         for (int e0 = t * per; e0 < total; e0 += NT * per) {
             int kk[ILP], jj[ILP], dk[ILP];
-            walk_fetch<NT, ILP>(G, sm, cnt, total, e0, per, j, kk, jj);
+            walk_fetch<NT, ILP, TOMB>(G, sm, cnt, total, e0, per, g, j, kk, jj);
             if (GATHER) {
                 gather_dist<ILP>(dr, kk, dk);
             } else {

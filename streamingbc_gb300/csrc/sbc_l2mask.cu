@@ -15,7 +15,8 @@
 //                    slot x -> z with z the root's neighbour i sets bit i of
 //                    mask[r][x]; an edge at the root flags the root.
 //   k_l2mask_remove  after an edge removal (thread per root): clears the bits
-//                    of the removed slots; an edge at the root flags it.
+//                    of the removed slots; an edge at the root flags it
+//                    (the _batch form: thread per (root, removal)).
 //   *_group          the same for several forests in one launch per step.
 // Masks describe the edges that existed when a batch began; the update adds
 // the edges its batch appended before the job (visible by seq) itself.
@@ -198,6 +199,33 @@ __global__ void k_l2mask_remove(const int64_t* __restrict__ roots, int nk, int u
     }
 }
 
+// After a batch of removals (undirected; code[i] == 1: removed): thread per
+// (root, deletion), as k_l2mask_remove does for one.
+__global__ void k_l2mask_remove_batch(const int64_t* __restrict__ roots, int nk, int n, const int32_t* __restrict__ iu,
+                                      const int32_t* __restrict__ iv, const int32_t* __restrict__ code, int64_t nv,
+                                      uint32_t* mask, const int32_t* __restrict__ cand,
+                                      const int32_t* __restrict__ l1n, int32_t* flag, int32_t* list, int32_t* cnt)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nk * n) return;
+    const int r = (int)(t / n), i = (int)(t % n);
+    if (code[i] != 1) return;
+    const int u = iu[i], v = iv[i];
+    const int root = (int)roots[r];
+    if (u == root || v == root) {
+        flag_rebuild(flag, list, cnt, r);
+        return;
+    }
+    const int c = l1n[r];
+    if (c < 0) return;
+    const int32_t* C = cand + (size_t)r * kL1Max;
+    uint32_t* M = mask + (size_t)r * nv;
+    const int bv = l1_index(C, c, v);
+    if (bv >= 0) atomicAnd(&M[u], ~(1u << bv));
+    const int bu = l1_index(C, c, u);
+    if (bu >= 0) atomicAnd(&M[v], ~(1u << bu));
+}
+
 namespace {
 
 // Rebuilds the flagged roots, then empties the list.
@@ -281,6 +309,21 @@ cudaError_t launch_l2mask_insert(sbc_graph* g, int n, bool directed)
     for (sbc_forest* f : g->forests) {
         cudaError_t e = launch_l2mask_insert_forest(f, n, directed, g->stream);
         if (e) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_l2mask_remove_batch(sbc_graph* g, int n)
+{
+    for (sbc_forest* f : g->forests) {
+        if (!f->d_l2mask || n <= 0) continue;
+        const int64_t threads = f->nk * (int64_t)n;
+        k_l2mask_remove_batch<<<(int)((threads + 255) / 256), 256, 0, g->stream>>>(
+            f->d_roots, (int)f->nk, n, g->d_ins, g->d_ins + g->ins_capacity, g->d_ins + 2 * g->ins_capacity, f->nv,
+            f->d_l2mask, f->d_l1cand, f->d_l1n, f->d_l2flag, f->d_l2list, f->d_l2cnt);
+        cudaError_t e = cudaGetLastError();
+        if (e) return e;
+        if ((e = rebuild_flagged(f, g->stream))) return e;
     }
     return cudaSuccess;
 }

@@ -34,6 +34,7 @@
 // reference only by floating-point summation order.
 #include <climits>
 #include <vector>
+#include "sbc_gb300.h"
 #include "sbc_host.h"
 #include "sbc_internal.cuh"
 #include "sbc_update_job.cuh"
@@ -45,6 +46,12 @@ struct UpdateArgs {
     ScratchBase scr;
     int all_visible;
     int del_u, del_v;  // k_delete: the deleted edge
+    int* mov;          // k_delete: roots left to a recompute
+    int* nmov;
+    int move_down;     // k_delete_batch: lost-parent roots move down (else recompute)
+    int* dirty;        // k_delete_batch: roots recomputed after the launch
+    int* dlist;
+    int* dcnt;
     const int* worklist;
     const int* nwork;
     int* work_counter;
@@ -73,7 +80,8 @@ __global__ void __launch_bounds__(NT, MINB) k_update(const __grid_constant__ Upd
 // Deletions (one launch per deletion, after k_classify_delete): its own
 // kernel, so the insertion kernel's code and registers are untouched; any
 // launch shape fits the forest's worker scratch, since it only indexes worker
-// slots below its grid.
+// slots below its grid.  Worklist entries carry kLostRoot for roots whose
+// deeper endpoint lost its last parent.
 template <int NT, int MINB, int ILP>
 __global__ void __launch_bounds__(NT, MINB) k_delete(const __grid_constant__ UpdateArgs A)
 {
@@ -87,9 +95,53 @@ __global__ void __launch_bounds__(NT, MINB) k_delete(const __grid_constant__ Upd
         const int item = sm.item;
         __syncthreads();
         if (item >= nwork) break;
-        process_deletion<NT, ILP>(A.f, sm, W, A.worklist[item], A.del_u, A.del_v);
+        const int w = A.worklist[item];
+        process_deletion<NT, ILP>(A.f, sm, W, w & ~kLostRoot, A.del_u, A.del_v, (w & kLostRoot) != 0, A.mov,
+                                  A.nmov);
     }
     flush_counters<NT>(sm, A.counters);
+}
+
+// A batch of deletions in one persistent launch: a CTA per active root runs
+// the batch's deletions in order on it (process_root_deletions).
+template <int NT, int MINB, int ILP>
+__global__ void __launch_bounds__(NT, MINB) k_delete_batch(const __grid_constant__ UpdateArgs A)
+{
+    __shared__ UpdSmem<NT> sm;
+    const Scratch W = A.scr.of(blockIdx.x, A.f.G.nv);
+    const int nwork = *A.nwork;
+    reset_counters<NT>(sm);
+    for (;;) {
+        if (threadIdx.x == 0) sm.item = atomicAdd(A.work_counter, 1);
+        __syncthreads();
+        const int item = sm.item;
+        __syncthreads();
+        if (item >= nwork) break;
+        process_root_deletions<NT, ILP>(A.f, sm, W, A.worklist[item], A.move_down != 0, A.dirty, A.dlist, A.dcnt);
+    }
+    flush_counters<NT>(sm, A.counters);
+}
+
+// Roots a batch of deletions can change: some removed edge joins two
+// different levels of the root's tree as the batch begins (while every
+// deletion so far was same-level the root is unchanged, so a root none of
+// whose deletions is different-level stays unchanged).  Warp per root, lanes
+// over the deletions.
+__global__ void k_classify_delete_batch(const int32_t* __restrict__ dist, int64_t nv, int nk, int n,
+                                        const int32_t* __restrict__ iu, const int32_t* __restrict__ iv,
+                                        const int32_t* __restrict__ code, int* __restrict__ worklist,
+                                        int* __restrict__ nwork)
+{
+    const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (r >= nk) return;
+    const int32_t* D = dist + (size_t)r * nv;
+    bool active = false;
+    for (int base = 0; base < n && !active; base += 32) {
+        const int i = base + lane;
+        active = __any_sync(0xffffffffu, i < n && code[i] == 1 && D[iu[i]] != D[iv[i]]);
+    }
+    if (lane == 0 && active) worklist[atomicAdd(nwork, 1)] = r;
 }
 
 __global__ void k_classify(const int32_t* __restrict__ dist, int64_t nv, int nk, int nins,
@@ -162,13 +214,14 @@ constexpr int kDefaultVariant = 7;
 // Deletion of (u, v), already removed from the adjacency: warp per root.  A
 // root whose endpoints sit on the same level (or are both unreachable) is
 // unaffected; otherwise the deeper endpoint b either keeps a parent (a
-// neighbour one level up) -- sigma-only update, work list -- or has none and
-// its subtree moves down -- recompute list (the reference's split,
-// src/streamingbc.c:300-345).
+// neighbour one level up) -- sigma-only update -- or has none and its subtree
+// moves down (the reference's split, src/streamingbc.c:300-345); the second
+// kind joins the work list flagged with kLostRoot (move_down) or the
+// recompute list mov.
 __global__ void k_classify_delete(const int32_t* __restrict__ dist, int64_t nv, int nk, DevGraph G, int u, int v,
                                   const int* __restrict__ removed, const int* __restrict__ dirty,
                                   int* __restrict__ adj, int* __restrict__ nadj, int* __restrict__ mov,
-                                  int* __restrict__ nmov, unsigned long long* counters)
+                                  int* __restrict__ nmov, int move_down, unsigned long long* counters)
 {
     const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -187,12 +240,9 @@ __global__ void k_classify_delete(const int32_t* __restrict__ dist, int64_t nv, 
         parent = __any_sync(0xffffffffu, s < db && D[G.col[rb + s]] == lb - 1);
     }
     if (lane == 0) {
-        if (parent) {
-            adj[atomicAdd(nadj, 1)] = r;
-        } else {
-            mov[atomicAdd(nmov, 1)] = r;
-            atomicAdd(&counters[3], 1ull);
-        }
+        if (parent || move_down) adj[atomicAdd(nadj, 1)] = parent ? r : (r | kLostRoot);
+        else mov[atomicAdd(nmov, 1)] = r;
+        if (!parent) atomicAdd(&counters[3], 1ull);
     }
 }
 
@@ -245,6 +295,7 @@ cudaError_t launch_update(sbc_forest* f, int n, bool all_visible)
     A.scr = f->scratch();
     A.all_visible = all_visible ? 1 : 0;
     A.del_u = A.del_v = 0;
+    A.mov = A.nmov = nullptr;
     A.worklist = f->d_worklist;
     A.nwork = f->d_nwork;
     A.work_counter = f->d_counter;
@@ -283,17 +334,23 @@ cudaError_t launch_delete_step(sbc_forest* f, int u, int v, const int* d_removed
     cudaError_t e;
     if ((e = cudaMemsetAsync(f->d_nwork, 0, 2 * sizeof(int), s)) || (e = cudaMemsetAsync(f->d_nmov, 0, 2 * sizeof(int), s)))
         return e;
+    const bool md = f->delete_mode == SBC_DELETE_MOVE_DOWN ||
+                    (f->delete_mode == SBC_DELETE_AUTO && f->nv >= kMoveDownMinVertices);
     k_classify_delete<<<(int)((f->nk * 32 + 255) / 256), 256, 0, s>>>(f->d_dist, f->nv, (int)f->nk, g->dev(), u, v,
                                                                       d_removed, f->d_dirty, f->d_worklist,
-                                                                      f->d_nwork, f->d_mov, f->d_nmov, f->d_counters);
+                                                                      f->d_nwork, f->d_mov, f->d_nmov, md ? 1 : 0,
+                                                                      f->d_counters);
     if ((e = cudaGetLastError())) return e;
-    // roots that keep a parent of the deeper endpoint: incremental
+    // roots that keep a parent: sigma-only update; the others move down (a
+    // move-down that outgrows its cap joins the recompute list mov)
     UpdateArgs A;
     A.f = forest_slot(f, 0);
     A.scr = f->scratch();
     A.all_visible = 1;
     A.del_u = u;
     A.del_v = v;
+    A.mov = f->d_mov;
+    A.nmov = f->d_nmov;
     A.worklist = f->d_worklist;
     A.nwork = f->d_nwork;
     A.work_counter = f->d_counter;
@@ -339,6 +396,37 @@ cudaError_t launch_delete_finish(sbc_forest* f)
     k_clear_dirty<<<(int)std::min<int64_t>((f->nk + 255) / 256, 64), 256, 0, s>>>(f->d_dlist, f->d_dcnt, f->d_dirty);
     if ((e = cudaGetLastError())) return e;
     return cudaMemsetAsync(f->d_dcnt, 0, sizeof(int), s);
+}
+
+cudaError_t launch_delete_batch(sbc_forest* f, int n)
+{
+    sbc_graph* g = f->g;
+    cudaStream_t s = g->stream;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(f->d_nwork, 0, 2 * sizeof(int), s))) return e;
+    const int32_t* iu = g->d_ins;
+    const int32_t* iv = g->d_ins + g->ins_capacity;
+    const int32_t* code = g->d_ins + 2 * g->ins_capacity;
+    k_classify_delete_batch<<<(int)((f->nk * 32 + 255) / 256), 256, 0, s>>>(f->d_dist, f->nv, (int)f->nk, n, iu, iv,
+                                                                            code, f->d_worklist, f->d_nwork);
+    if ((e = cudaGetLastError())) return e;
+    UpdateArgs A;
+    A.f = forest_slot(f, n);
+    A.scr = f->scratch();
+    A.all_visible = 1;
+    A.del_u = A.del_v = 0;
+    A.mov = A.nmov = nullptr;
+    A.move_down = (f->delete_mode == SBC_DELETE_MOVE_DOWN ||
+                   (f->delete_mode == SBC_DELETE_AUTO && f->nv >= kMoveDownMinVertices)) ? 1 : 0;
+    A.dirty = f->d_dirty;
+    A.dlist = f->d_dlist;
+    A.dcnt = f->d_dcnt;
+    A.worklist = f->d_worklist;
+    A.nwork = f->d_nwork;
+    A.work_counter = f->d_counter;
+    A.counters = f->d_counters;
+    k_delete_batch<512, 1, 4><<<(int)std::min<int64_t>(f->workers, f->nk), 512, 0, s>>>(A);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_delete(sbc_forest* f, int u, int v, const int* d_removed)

@@ -27,6 +27,10 @@ struct UpdSmem {
 // many times the root's degree; a probe is costed as this many scanned slots.
 constexpr int kProbeRatio = 32;
 
+template <int NT, int ILP, bool DECR, bool TOMB>
+__device__ __forceinline__ void ascend(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r, int a, int b,
+                                       bool moving, int g, bool del, int Lb, int nsteps, int ndown);
+
 // One job: the insertion of edge (a, b) (a the shallower endpoint) on root r,
 // or with `del` the deletion of that edge when b keeps another parent (the
 // edge is already gone from the adjacency; |d| == 1, levels do not change).
@@ -34,20 +38,15 @@ constexpr int kProbeRatio = 32;
 // taken away (diffPath -sigma[a]) and, since b no longer reaches a through
 // the adjacency, b's old contribution to a taken out when b is committed
 // (removeEdgeWithoutMovementBrandes, src/streamingbc_internal.c:607-868).
-template <int NT, int ILP>
+template <int NT, int ILP, bool TOMB = false>
 __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r,
                                         int a, int b, bool moving, int g, bool del = false)
 {
     const int64_t nv = A.G.nv;
-    const uint32_t* M2 = sm.mask_ok ? A.l2mask + (size_t)r * nv : nullptr;
-    const int32_t* C1 = sm.mask_ok ? A.l1cand + (size_t)r * kL1Max : nullptr;
-    const int n1 = sm.mask_ok ? A.l1n[r] : 0;
     int32_t* D = A.dist + (size_t)r * nv;
     uint8_t* D8 = A.dist8 + (size_t)r * nv;
     uint32_t* D2 = A.dist2 + (size_t)r * d2_words(nv);
-    int64_t* S = A.sigma + (size_t)r * nv;
-    double* Dl = A.delta + (size_t)r * nv;
-    const int root = (int)A.roots[r];
+    const int64_t* S = A.sigma + (size_t)r * nv;
     const int Lb = D[a] + 1;  // new level of b; equals D[b] when |d| == 1
 
     if (threadIdx.x == 0) {
@@ -70,7 +69,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
         const int L = Lb + step;
         const int tag = step + 2;
         // a re-levelling descent compares old distances far from L: one-byte row
-        lb_walk<NT, true, ILP>(
+        lb_walk<NT, true, ILP, TOMB>(
             A.G, g, DistRow{D, D8, moving ? nullptr : D2, L}, W.qd + lo, hi - lo, nullptr, 0, sm.lb,
             [&](int j, int x, int d) { sm.dp[j] = W.dp[x]; },
             [&](int j, int x, int k, int dk) {
@@ -125,6 +124,32 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
         }
     }
     __syncthreads();
+    ascend<NT, ILP, false, TOMB>(A, sm, W, r, a, b, moving, g, del, Lb, nsteps, ndown);
+}
+
+// The dependency ascent of a job, from the deepest level its descent touched
+// (descent vertices listed by level in W.qd / W.lvl, their st tags, sigma
+// changes in W.dp) up to the root, then the reset of the touched scratch.
+// DECR: the job is a deletion whose deeper endpoint b lost its last parent
+// (movedown below): the moved vertices went DOWN, so an unmoved parent of a
+// moved vertex is a parent it gained (its full new weight, not a difference),
+// no same-level ex-parent loses a child, and a (not in the descent) loses b's
+// old weight, seeded in W.acc[a] and queued when the walk reaches level D[a].
+template <int NT, int ILP, bool DECR, bool TOMB>
+__device__ __forceinline__ void ascend(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r, int a, int b,
+                                       bool moving, int g, bool del, int Lb, int nsteps, int ndown)
+{
+    const int64_t nv = A.G.nv;
+    const uint32_t* M2 = sm.mask_ok ? A.l2mask + (size_t)r * nv : nullptr;
+    const int32_t* C1 = sm.mask_ok ? A.l1cand + (size_t)r * kL1Max : nullptr;
+    const int n1 = sm.mask_ok ? A.l1n[r] : 0;
+    int32_t* D = A.dist + (size_t)r * nv;
+    uint8_t* D8 = A.dist8 + (size_t)r * nv;
+    uint32_t* D2 = A.dist2 + (size_t)r * d2_words(nv);
+    int64_t* S = A.sigma + (size_t)r * nv;
+    double* Dl = A.delta + (size_t)r * nv;
+    const int root = (int)A.roots[r];
+    const int aL = DECR ? D[a] : 0;
 
     // ---------------- ascent ----------------
     // A parent k's delta gains, per child x, sigma_k * (newdelta_x+1)/newsigma_x,
@@ -152,7 +177,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
         if (x != root) atomicAdd(&A.bc[x], nD - oD);
         S[x] = nS;
         Dl[x] = nD;
-        if (del && x == b) {
+        if (!DECR && del && x == b) {
             // a (one level up, not in the descent) loses b's old contribution
             int old = atomicOr(&W.st[a], SBC_ASC);
             if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = a;
@@ -180,7 +205,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
             const int old = atomicOr(&W.st[k], SBC_ASC);
             warp_append(&sm.at, W.qa, k, !(old & SBC_ASC));
         }
-        const bool fresh = kDown || (k == a && (sm.fl[j] & 2));
+        const bool fresh = kDown || (k == a && (sm.fl[j] & 2)) || (DECR && (sm.fl[j] & 1));
         atomicAdd(&W.acc[k], fresh ? sm.wn[j] : sm.wd[j]);
         return true;
     };
@@ -198,15 +223,18 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
     // candidate parent tests a neighbour with one (L2-resident) bit instead of
     // gathering its distance and state.
     auto pull_walk = [&](const int32_t* plist, int pn) {
-        lb_walk_sum<NT, false, ILP>(
+        lb_walk_sum<NT, false, ILP, TOMB>(
             A.G, g, DistRow{D, D8, nullptr, 0}, plist, pn, sm.lb, sm.wn, sm.fl,
             [&](int j, int y, int d) {
                 const int sy = W.st[y];
-                sm.fl[j] = ((sy & SBC_STEP_MASK) ? 1 : 0) | (y == a ? 2 : 0);
+                // a root neighbour whose edge a batched deletion already took
+                // is no longer at level 1 (and no parent)
+                sm.fl[j] = ((sy & SBC_STEP_MASK) ? 1 : 0) | (y == a ? 2 : 0) | (TOMB && D8[y] != 1 ? 8 : 0);
             },
             [&](int j, int y, int c, int, double& v) -> bool {
                 if (!((W.bits[c >> 5] >> (c & 31)) & 1u)) return false;
                 const int fl = sm.fl[j];
+                if (fl & 8) return false;
                 const bool fresh = (fl & 1) || ((fl & 2) && c == b);
                 v = fresh ? W.acc[c] : __longlong_as_double((long long)W.dp[c]);
                 return true;
@@ -239,17 +267,18 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
             const int vx = vis_deg(A.G, x, rx, g);
             const double wn = W.acc[x];
             const double wd = __longlong_as_double((long long)W.dp[x]);
+            const bool xm = DECR && (W.st[x] & SBC_MOVED);
             for (int t = lane; t < ncand; t += 32) {
                 const int y = cand[t];
                 if (check && D8[y] != L - 1) continue;
-                if (!has_edge(A.G, x, rx, vx, y, cost)) continue;
+                if (!has_edge<TOMB>(A.G, x, rx, vx, y, g, cost)) continue;
                 const int sy = W.st[y];
                 const bool yDown = (sy & SBC_STEP_MASK) != 0;
                 if (!yDown && !(sy & SBC_ASC)) {
                     const int old = atomicOr(&W.st[y], SBC_ASC);
                     warp_append(&sm.at, W.qa, y, !(old & SBC_ASC));
                 }
-                atomicAdd(&W.acc[y], (yDown || (y == a && x == b)) ? wn : wd);
+                atomicAdd(&W.acc[y], (yDown || xm || (y == a && x == b)) ? wn : wd);
             }
         }
         if (cost) atomicAdd(&sm.lb.scanned_e, (unsigned long long)cost);
@@ -321,14 +350,14 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
             const int32_t* nl2 = W.qa + ua_lo;
             int nn1 = dn, nn2 = ua_hi - ua_lo;
             bool near = pull_ok;
-            if (!pull_ok && !moving) {
-                lb_walk<NT, true, ILP>(A.G, g, DistRow{D, D8, D2, L}, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb,
+            if (!pull_ok && (!moving || DECR)) {
+                lb_walk<NT, true, ILP, TOMB>(A.G, g, DistRow{D, D8, D2, L}, dlist, dn, W.qa + ua_lo, ua_hi - ua_lo, sm.lb,
                                        prep_div,
                                        [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
                 probe_diverted();
             } else if (!pull_ok) {
                 const int same_lo = sm.st;
-                lb_walk<NT, true, ILP>(
+                lb_walk<NT, true, ILP, TOMB>(
                     A.G, g, DistRow{D, D8, D2, L}, dlist, dn, nullptr, 0, sm.lb, prep,
                     [&](int j, int x, int k, int dk) {
                         if (parent_edge(j, x, k, dk)) return;
@@ -354,7 +383,7 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                     nl2 = W.qs + same_lo;
                     nn2 = same_hi - same_lo;
                 } else {
-                    lb_walk<NT, true, ILP>(A.G, g, DistRow{D, D8, D2, L}, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo,
+                    lb_walk<NT, true, ILP, TOMB>(A.G, g, DistRow{D, D8, D2, L}, W.qa + ua_lo, ua_hi - ua_lo, W.qs + same_lo,
                                            same_hi - same_lo, sm.lb, prep_div,
                                            [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
                     probe_diverted();
@@ -456,10 +485,10 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                         pull_walk(A.G.col + rrow, rdeg);
                     } else {
                         const int nscan = sm.nscan, nprobe = sm.nprobe;
-                        lb_walk<NT, false, ILP>(A.G, g, DistRow{D, D8, D2, L}, W.qs + qbase, nscan, nullptr, 0, sm.lb,
+                        lb_walk<NT, false, ILP, TOMB>(A.G, g, DistRow{D, D8, D2, L}, W.qs + qbase, nscan, nullptr, 0, sm.lb,
                                                 prep_loaded,
                                            [&](int j, int x, int k, int dk) { parent_edge(j, x, k, dk); }, NoPost());
-                        probe_parents(W.qs + nv - nprobe, nprobe, A.G.col + rrow, rdeg, false);
+                        probe_parents(W.qs + nv - nprobe, nprobe, A.G.col + rrow, rdeg, TOMB);
                     }
                     for (int i = threadIdx.x; i < nn1 + nn2; i += NT) {
                         const int x = i < nn1 ? nl1[i] : nl2[i - nn1];
@@ -469,9 +498,17 @@ __device__ __forceinline__ void run_job(const ForestSlot& A, UpdSmem<NT>& sm, co
                 }
             }
         }
+        if (DECR && L == aL + 1) {
+            // a lost b's old weight (seeded in acc[a]): walked at its level
+            if (threadIdx.x == 0) {
+                const int old = atomicOr(&W.st[a], SBC_ASC);
+                if (!(old & SBC_ASC)) W.qa[atomicAdd(&sm.at, 1)] = a;
+            }
+            __syncthreads();
+        }
         ua_lo = next_lo;
         ua_hi = sm.at;
-        if (L <= Lb && ua_lo == ua_hi) break;
+        if (L <= Lb && ua_lo == ua_hi && (!DECR || L <= aL + 1)) break;
     }
 
     // ---------------- reset touched scratch ----------------
@@ -537,22 +574,380 @@ __device__ __forceinline__ void process_root(const ForestSlot& A, UpdSmem<NT>& s
     }
 }
 
-// The deletion of (u, v) on root r, which keeps a parent of the deeper
-// endpoint (the classify step sends the other roots to a recompute).
+// Deletion worklist entries: root index | kLostRoot when the deeper endpoint
+// has no parent left.
+constexpr int kLostRoot = 0x40000000;
+
+// Scratch states of a move-down job (bits outside SBC_STEP_MASK, SBC_MOVED and
+// SBC_ASC; cleared before its ascent).
+constexpr int kDecUp = 0x04000000;    // candidate with a parent outside the affected set
+constexpr int kDecAff = 0x20000000;   // in the affected set: its level grows
+constexpr int kDecCand = 0x40000000;  // child of an affected vertex, tested for another parent
+
+// Affected sets larger than this are left to a recompute of the root.
+__device__ __forceinline__ int movedown_cap(int64_t nv) { return (int)max((int64_t)1024, nv / 16); }
+
+// Block-wide minimum (op 0) or maximum (op 1) of v over the threads; *cell is
+// a shared int the block may overwrite.
+template <int NT>
+__device__ __forceinline__ int block_minmax(int v, int* cell, int op)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) *cell = op ? INT_MIN : INT_MAX;
+    __syncthreads();
+    if (op ? v > INT_MIN : v < INT_MAX) {
+        if (op) atomicMax(cell, v);
+        else atomicMin(cell, v);
+    }
+    __syncthreads();
+    const int out = *cell;
+    __syncthreads();
+    return out;
+}
+
+// Deletion of (a, b) (already gone from the adjacency) on root r where b, one
+// level below a, had a as its only parent: b and possibly part of its subtree
+// move down (moveDownTreeBrandes, src/streamingbc_internal.c:880-1401, whose
+// result disagrees with a recompute; this one is exact):
+//   1. affected set X, by old level from b: a child of X all of whose parents
+//      are in X joins X; the other children ("boundary") keep their level and
+//      lose the paths through their parents in X (sigma change -sum sigma).
+//   2. new levels of X: 1 + the lowest unaffected neighbour, then relaxed
+//      inside X in level order (unit-weight Dijkstra); none: unreachable.
+//   3. level by level from D[b] + 1: sigma of the X vertices from their new
+//      parents, and the sigma changes of the boundary pushed down to the
+//      unaffected children (an X vertex never parents an unaffected one, since
+//      its new level exceeds its old one and neighbours' old levels differ by
+//      at most one), listing every changed vertex by level as a descent does.
+//   4. X re-levelled (unreachable ones leave BC and get sigma 0), then the
+//      shared ascent with the move-down rules.
+// Returns false, with the root's state untouched and the scratch clean, when
+// X outgrows movedown_cap: the root is then recomputed.
+template <int NT, int ILP, bool TOMB>
+__device__ bool movedown(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r, int a, int b, int g)
+{
+    const int64_t nv = A.G.nv;
+    int32_t* D = A.dist + (size_t)r * nv;
+    uint8_t* D8 = A.dist8 + (size_t)r * nv;
+    uint32_t* D2 = A.dist2 + (size_t)r * d2_words(nv);
+    int64_t* S = A.sigma + (size_t)r * nv;
+    double* Dl = A.delta + (size_t)r * nv;
+    const int root = (int)A.roots[r];
+    const int lb = D[b];
+    const double wb = (Dl[b] + 1.0) / (double)S[b];  // b's old weight, which a loses
+    const DistRow row{D, D8, nullptr, 0};
+    auto noprep = [](int, int, int) {};
+    if (threadIdx.x == 0) {
+        W.st[b] = kDecAff;
+        W.qs[0] = b;
+        sm.st = 1;  // X, in W.qs
+        sm.at = 0;  // candidates, in W.qa
+        sm.qt = 0;
+    }
+    __syncthreads();
+
+    // ---- 1. affected set ----
+    int lo = 0, hi = 1, l = lb;
+    bool over = false;
+    while (lo < hi) {
+        const int c_lo = sm.at;
+        lb_walk<NT, false, ILP, TOMB>(A.G, g, row, W.qs + lo, hi - lo, nullptr, 0, sm.lb, noprep,
+                                [&](int, int, int k, int dk) {
+                                    if (dk != l + 1 || W.st[k] != 0) return;
+                                    const int old = atomicCAS(&W.st[k], 0, kDecCand);
+                                    warp_append(&sm.at, W.qa, k, old == 0);
+                                },
+                                NoPost());
+        const int c_hi = sm.at;
+        lb_walk<NT, false, ILP, TOMB>(A.G, g, row, W.qa + c_lo, c_hi - c_lo, nullptr, 0, sm.lb, noprep,
+                                [&](int, int k, int y, int dy) {
+                                    if (dy != l) return;
+                                    if (W.st[y] & kDecAff) atomic_add_i64(&W.dp[k], S[y]);
+                                    else if (!(W.st[k] & kDecUp)) atomicOr(&W.st[k], kDecUp);
+                                },
+                                NoPost());
+        for (int i = c_lo + threadIdx.x; i < c_hi; i += NT) {
+            const int k = W.qa[i];
+            const bool in = !(W.st[k] & kDecUp);
+            if (in) {
+                W.st[k] = kDecAff;
+                W.dp[k] = 0;
+            } else {
+                W.dp[k] = -W.dp[k];  // boundary: sigma change so far
+            }
+            warp_append(&sm.st, W.qs, k, in);
+        }
+        __syncthreads();
+        lo = hi;
+        hi = sm.st;
+        ++l;
+        if (hi > movedown_cap(nv)) {
+            over = true;
+            break;
+        }
+    }
+    const int nx = sm.st, nc = sm.at;
+    if (over) {
+        for (int i = threadIdx.x; i < nx; i += NT) {
+            W.st[W.qs[i]] = 0;
+            W.dp[W.qs[i]] = 0;
+        }
+        for (int i = threadIdx.x; i < nc; i += NT) {
+            W.st[W.qa[i]] = 0;
+            W.dp[W.qa[i]] = 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) sm.st = sm.at = 0;
+        __syncthreads();
+        return false;
+    }
+
+    // ---- 2. new levels of X (held in the step bits; SBC_STEP_MASK = none) ----
+    for (int i = threadIdx.x; i < nx; i += NT) W.st[W.qs[i]] = kDecAff | SBC_STEP_MASK;
+    __syncthreads();
+    lb_walk<NT, false, ILP, TOMB>(A.G, g, row, W.qs, nx, nullptr, 0, sm.lb, noprep,
+                            [&](int, int x, int y, int dy) {
+                                if (dy == SBC_INF || (W.st[y] & kDecAff)) return;
+                                const int want = kDecAff | (dy + 1);
+                                if (want < W.st[x]) atomicMin(&W.st[x], want);
+                            },
+                            NoPost());
+    int tl = INT_MAX;
+    for (int i = threadIdx.x; i < nx; i += NT) tl = min(tl, W.st[W.qs[i]] & SBC_STEP_MASK);
+    int L = block_minmax<NT>(tl, &sm.nprobe, 0);
+    int tmax = 0;
+    while (L < SBC_STEP_MASK) {
+        tmax = L;
+        if (threadIdx.x == 0) sm.qt = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < nx; i += NT) {
+            const int x = W.qs[i];
+            warp_append(&sm.qt, W.qd, x, (W.st[x] & SBC_STEP_MASK) == L);
+        }
+        __syncthreads();
+        lb_walk<NT, false, ILP, TOMB>(A.G, g, row, W.qd, sm.qt, nullptr, 0, sm.lb, noprep,
+                                [&](int, int, int z, int) {
+                                    const int sz = W.st[z];
+                                    if ((sz & kDecAff) && (sz & SBC_STEP_MASK) > L + 1)
+                                        atomicMin(&W.st[z], kDecAff | (L + 1));
+                                },
+                                NoPost());
+        tl = INT_MAX;
+        for (int i = threadIdx.x; i < nx; i += NT) {
+            const int t = W.st[W.qs[i]] & SBC_STEP_MASK;
+            if (t > L) tl = min(tl, t);
+        }
+        L = block_minmax<NT>(tl, &sm.nprobe, 0);
+    }
+
+    // ---- 3. sigma by level ----
+    const int Lb = lb + 1;  // no vertex above this level changes
+    for (int i = threadIdx.x; i < nx; i += NT) {
+        const int x = W.qs[i];
+        const int t = W.st[x] & SBC_STEP_MASK;
+        W.st[x] = kDecAff | (t == SBC_STEP_MASK ? 0 : t - Lb + 1);  // tag of the new level; 0: unreachable
+    }
+    int um = INT_MIN;
+    for (int i = threadIdx.x; i < nc; i += NT) {
+        const int k = W.qa[i];
+        if (!(W.st[k] & kDecAff)) um = max(um, D[k]);
+    }
+    const int Lend = max(block_minmax<NT>(um, &sm.nprobe, 1), tmax);
+    if (threadIdx.x == 0) {
+        sm.qt = 0;
+        W.lvl[0] = 0;
+    }
+    __syncthreads();
+    int step = 0;
+    for (int Lc = Lb;; ++Lc, ++step) {
+        const int tag = step + 1;
+        const int p_hi = sm.qt;  // vertices pushed to this level by the previous one
+        __syncthreads();
+        for (int i = threadIdx.x; i < nx; i += NT) {
+            const int x = W.qs[i];
+            warp_append(&sm.qt, W.qd, x, (W.st[x] & SBC_STEP_MASK) == tag);
+        }
+        __syncthreads();
+        const int x_hi = sm.qt;
+        __syncthreads();
+        for (int i = threadIdx.x; i < nc; i += NT) {
+            const int k = W.qa[i];
+            const int s = W.st[k];
+            const bool take = !(s & kDecAff) && !(s & SBC_STEP_MASK) && D[k] == Lc;
+            if (take) W.st[k] = s | tag;
+            warp_append(&sm.qt, W.qd, k, take);
+        }
+        __syncthreads();
+        const int end = sm.qt;
+        const int seg_lo = W.lvl[step];
+        if (threadIdx.x == 0) W.lvl[step + 1] = end;
+        // X vertices of this level: sigma from the new parents one level up
+        lb_walk<NT, false, ILP, TOMB>(A.G, g, row, W.qd + p_hi, x_hi - p_hi, nullptr, 0, sm.lb, noprep,
+                                [&](int, int x, int y, int dy) {
+                                    const int sy = W.st[y];
+                                    int ly;
+                                    int64_t sg;
+                                    if (sy & kDecAff) {
+                                        const int ty = sy & SBC_STEP_MASK;
+                                        if (ty == 0) return;
+                                        ly = Lb + ty - 1;
+                                        sg = W.dp[y];
+                                    } else {
+                                        ly = dy;
+                                        sg = S[y] + ((sy & SBC_STEP_MASK) ? W.dp[y] : 0);
+                                    }
+                                    if (ly == Lc - 1) atomic_add_i64(&W.dp[x], sg);
+                                },
+                                NoPost());
+        // unaffected vertices of this level: their sigma changes to their
+        // unaffected children (never to an X vertex)
+        lb_walk<NT, false, ILP, TOMB>(
+            A.G, g, row, W.qd + seg_lo, p_hi - seg_lo, W.qd + x_hi, end - x_hi, sm.lb,
+            [&](int j, int x, int) { sm.dp[j] = W.dp[x]; },
+            [&](int j, int, int k, int dk) {
+                if (dk != Lc + 1) return;
+                int s = W.st[k];
+                if (s & kDecAff) return;
+                if (!(s & SBC_STEP_MASK)) {
+                    const int old = atomicCAS(&W.st[k], s, s | (tag + 1));
+                    warp_append(&sm.qt, W.qd, k, old == s);
+                    s = old == s ? (s | (tag + 1)) : old;
+                }
+                if ((s & SBC_STEP_MASK) != tag + 1) return;
+                atomic_add_i64(&W.dp[k], sm.dp[j]);
+            },
+            NoPost());
+        if (sm.qt == end && Lc >= Lend) {
+            ++step;
+            break;
+        }
+    }
+    const int nsteps = step, ndown = sm.qt;
+
+    // ---- 4. re-level X, then the ascent ----
+    for (int i = threadIdx.x; i < nc; i += NT) {
+        const int k = W.qa[i];
+        const int s = W.st[k];
+        if (!(s & kDecAff)) W.st[k] = s & SBC_STEP_MASK;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nx; i += NT) {
+        const int x = W.qs[i];
+        const int tag = W.st[x] & SBC_STEP_MASK;
+        const int old = D[x];
+        const int nl = tag ? Lb + tag - 1 : SBC_INF;
+        if (A.lvlhist) {
+            int32_t* H = A.lvlhist + (size_t)r * kHistLevels;
+            atomicSub(&H[min(old, kHistLevels - 1)], 1);
+            if (tag) atomicAdd(&H[min(nl, kHistLevels - 1)], 1);
+        }
+        if (A.roster) {
+            const size_t rb = (size_t)r * kRosterLevels;
+            if (tag && nl >= 2 && nl < kRosterLevels && A.roster_n[rb + nl] <= kRosterCap) {
+                const int p = atomicAdd(&A.roster_n[rb + nl], 1);
+                if (p < kRosterCap) A.roster[(rb + nl) * kRosterCap + p] = x;
+            }
+            if (old >= 2 && old < kRosterLevels && A.roster_n[rb + old] <= kRosterCap) A.roster_dirty[rb + old] = 1;
+        }
+        D[x] = nl;
+        D8[x] = enc_d8(nl);
+        set_d2(D2, x, nl);
+        if (tag) {
+            W.st[x] = tag | SBC_MOVED;
+        } else {
+            // unreachable now: out of BC, no paths
+            if (x != root) atomicAdd(&A.bc[x], -Dl[x]);
+            S[x] = 0;
+            Dl[x] = 0.0;
+            W.st[x] = 0;
+            W.dp[x] = 0;
+        }
+    }
+    if (threadIdx.x == 0) {
+        W.acc[a] = -wb;
+        sm.at = 0;
+        sm.st = nx;  // X stays listed in W.qs for the final reset
+        sm.nscan = sm.nprobe = 0;
+    }
+    __syncthreads();
+    ascend<NT, ILP, true, TOMB>(A, sm, W, r, a, b, true, g, true, Lb, nsteps, ndown);
+    return true;
+}
+
+// The deletion of (u, v) on root r.  lost: the deeper endpoint has no parent
+// left (the classify step's split); such a root moves down, or, when that
+// fails, joins the recompute list mov.
 template <int NT, int ILP>
 __device__ __forceinline__ void process_deletion(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r,
-                                                 int u, int v)
+                                                 int u, int v, bool lost, int* mov, int* nmov)
 {
     const int32_t* D = A.dist + (size_t)r * A.G.nv;
     const int du = D[u], dv = D[v];
     if (du == dv) return;
     // the masks were brought up to date with the removal before this launch
     if (threadIdx.x == 0) {
-        sm.c1 += 1;
+        if (!lost) sm.c1 += 1;
         sm.mask_ok = (A.l2mask && A.l1n[r] >= 0) ? 1 : 0;
     }
     __syncthreads();
-    run_job<NT, ILP>(A, sm, W, r, du < dv ? u : v, du < dv ? v : u, false, INT_MAX, true);
+    const int a = du < dv ? u : v, b = du < dv ? v : u;
+    if (!lost) {
+        run_job<NT, ILP>(A, sm, W, r, a, b, false, INT_MAX, true);
+    } else if (!movedown<NT, ILP, false>(A, sm, W, r, a, b, INT_MAX)) {
+        if (threadIdx.x == 0) mov[atomicAdd(nmov, 1)] = r;
+    }
+}
+
+// Every deletion of a batch applied in order to root r.  The batch's removed
+// slots are still in place, marked (slot_live<true>), so deletion i's jobs see
+// the graph without the edges of deletions 0..i, as one-at-a-time deletions
+// would.  Per deletion, on the root's current levels: endpoints on one level
+// change nothing; else the deeper endpoint b keeps a parent (sigma-only job)
+// or not (move-down).  Without move-down (or when it outgrows its cap) the
+// root's dependencies (exact for the graph before deletion i) leave BC, the
+// root joins the dirty list and skips the batch's later deletions; it is
+// recomputed on the final graph after the launch.  The level-2 masks describe
+// the graph before the batch and are not used.
+template <int NT, int ILP>
+__device__ __forceinline__ void process_root_deletions(const ForestSlot& A, UpdSmem<NT>& sm, const Scratch& W, int r,
+                                                       bool move_down, int* dirty, int* dlist, int* dcnt)
+{
+    const int64_t nv = A.G.nv;
+    const int32_t* D = A.dist + (size_t)r * nv;
+    if (threadIdx.x == 0) sm.mask_ok = 0;
+    __syncthreads();
+    for (int i = 0; i < A.nins; ++i) {
+        if (A.ins_ok[i] != 1) continue;
+        const int u = A.ins_u[i], v = A.ins_v[i];
+        const int du = D[u], dv = D[v];
+        if (du == dv) continue;
+        const int a = du < dv ? u : v, b = du < dv ? v : u;
+        const int lb = max(du, dv);
+        const int64_t rb = A.G.row[b];
+        const int db = A.G.deg[b];
+        int has = 0;
+        for (int s = threadIdx.x; s < db && !has; s += NT)
+            if (D[A.G.col[rb + s]] == lb - 1 && slot_live<true>(A.G, rb + s, i)) has = 1;
+        if (__syncthreads_or(has)) {
+            if (threadIdx.x == 0) sm.c1 += 1;
+            run_job<NT, ILP, true>(A, sm, W, r, a, b, false, i, true);
+            continue;
+        }
+        if (threadIdx.x == 0) sm.c2 += 1;
+        if (move_down && movedown<NT, ILP, true>(A, sm, W, r, a, b, i)) continue;
+        const int root = (int)A.roots[r];
+        const double* Dl = A.delta + (size_t)r * nv;
+        for (int64_t x = threadIdx.x; x < nv; x += NT) {
+            const double d = Dl[x];
+            if (d != 0.0 && x != root) atomicAdd(&A.bc[x], -d);
+        }
+        if (threadIdx.x == 0) {
+            dirty[r] = 1;
+            dlist[atomicAdd(dcnt, 1)] = r;
+        }
+        __syncthreads();
+        break;
+    }
 }
 
 // Zeroes the CTA's traversal and case counters (thread 0, before the first barrier).

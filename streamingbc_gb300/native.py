@@ -115,6 +115,7 @@ def load(path: str = LIB_PATH):
         "sbc_set_graph_capture": (C.c_int, [_vp, C.c_int]),
         "sbc_forest_set_variant": (C.c_int, [_vp, C.c_int]),
         "sbc_forest_variant": (C.c_int, [_vp, C.POINTER(C.c_int)]),
+        "sbc_forest_set_delete_mode": (C.c_int, [_vp, C.c_int]),
         "sbc_forest_autotune": (C.c_int, [_vp, C.c_int64, _i64p, _i64p, C.c_int, C.POINTER(C.c_int), _f64p,
                                           C.c_int]),
         "sbc_cost_model_size": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -415,6 +416,13 @@ class DeviceForest:
         st = BatchStats()
         _check(self.lib.sbc_delete_batch(self.h, u.size, p64(u), p64(v), C.byref(st)))
         return st.as_dict()
+
+    DELETE_AUTO, DELETE_MOVE_DOWN, DELETE_RECOMPUTE = 0, 1, 2
+
+    def set_delete_mode(self, mode: int) -> None:
+        """How roots whose deeper endpoint loses its last parent are updated:
+        moved down in place, recomputed after the call, or by graph size."""
+        _check(self.lib.sbc_forest_set_delete_mode(self.h, int(mode)))
 
     def update_deleted(self, u: int, v: int) -> dict:
         """The update for a deletion whose edge was already removed from the graph."""

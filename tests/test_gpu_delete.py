@@ -12,6 +12,10 @@ from streamingbc_gb300 import native
 
 pytestmark = pytest.mark.gpu
 
+MOVE_DOWN = native.DeviceForest.DELETE_MOVE_DOWN
+RECOMPUTE = native.DeviceForest.DELETE_RECOMPUTE
+both_modes = pytest.mark.parametrize("mode", [MOVE_DOWN, RECOMPUTE], ids=["move_down", "recompute"])
+
 
 def _edges(g):
     src = np.repeat(np.arange(g.nv), np.diff(g.off))
@@ -25,7 +29,8 @@ def _check(f, o):
     assert_bc(f.bc(), o.bc())
 
 
-def test_deletions_one_at_a_time_exact_er(sbc_lib, port_lib):
+@both_modes
+def test_deletions_one_at_a_time_exact_er(sbc_lib, port_lib, mode):
     """ER 200/800, exact BC (K = 200): 40 deletions, state after each."""
     g = G.er(200, 800, seed=5)
     roots = G.pick_roots(g.nv, g.nv, seed=5)
@@ -35,6 +40,7 @@ def test_deletions_one_at_a_time_exact_er(sbc_lib, port_lib):
     o.static()
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
     f = native.DeviceForest(dg, roots)
+    f.set_delete_mode(mode)
     f.static_init()
     moved = adjacent = 0
     for u, v in dels:
@@ -44,12 +50,13 @@ def test_deletions_one_at_a_time_exact_er(sbc_lib, port_lib):
         moved += st["case2"]
         adjacent += st["case1"]
         _check(f, o)
-    assert moved > 0 and adjacent > 0  # both the incremental and the recompute path ran
+    assert moved > 0 and adjacent > 0  # both kinds of affected root met
     f.close()
     dg.close()
 
 
-def test_rmat_deletions_between_insertion_batches(sbc_lib, port_lib):
+@both_modes
+def test_rmat_deletions_between_insertion_batches(sbc_lib, port_lib, mode):
     """R-MAT scale 10 with degree-1 roots (rosters in use): insertion batches
     and deletions (of original and of newly inserted edges) interleaved."""
     g = G.rmat(10, 8, seed=9)
@@ -63,6 +70,7 @@ def test_rmat_deletions_between_insertion_batches(sbc_lib, port_lib):
     o.static()
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
     f = native.DeviceForest(dg, roots)
+    f.set_delete_mode(mode)
     f.static_init()
     for k in range(3):
         batch = ins[32 * k:32 * (k + 1)]
@@ -106,6 +114,7 @@ def test_caller_removes_then_updates(sbc_lib, port_lib):
     o.static()
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
     f = native.DeviceForest(dg, roots)
+    f.set_delete_mode(MOVE_DOWN)
     f.static_init()
     for u, v in _edges(g)[:20]:
         assert dg.remove_directed(u, v) == 1 and dg.remove_directed(v, u) == 1
@@ -146,10 +155,11 @@ def test_rmat16_deletions_equal_static_recompute(sbc_lib):
     dg2.close()
 
 
-def test_bridge_deletions_recompute_many_roots(sbc_lib, port_lib):
+@both_modes
+def test_bridge_deletions_many_roots(sbc_lib, port_lib, mode):
     """A random tree plus a few chords: deleting a bridge leaves the deeper
-    endpoint without a parent for most roots, so one deletion recomputes many
-    roots at once (the static kernel path on small graphs)."""
+    endpoint without a parent for most roots, so one deletion moves many roots'
+    subtrees down at once (cutting them off the root), or recomputes them."""
     rng = np.random.default_rng(12)
     n = 300
     par = np.array([rng.integers(0, i) for i in range(1, n)])
@@ -163,6 +173,7 @@ def test_bridge_deletions_recompute_many_roots(sbc_lib, port_lib):
     o.static()
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
     f = native.DeviceForest(dg, roots)
+    f.set_delete_mode(mode)
     f.static_init()
     most = 0
     for u, v in list(tree[rng.choice(len(tree), 6, replace=False)]) + list(_edges(g)[:6]):
@@ -177,9 +188,9 @@ def test_bridge_deletions_recompute_many_roots(sbc_lib, port_lib):
 
 
 def test_wide_recompute_on_large_graph(sbc_lib):
-    """On a graph of >= 32768 vertices a deletion recomputes its few affected
-    roots with the whole GPU; the result equals a static init of the graph
-    without the edges."""
+    """Chung-Lu 40k: deletions of leaf edges (the leaf leaves every root's
+    tree) and of random edges in one call; the result equals a static init of
+    the graph without the edges."""
     g = G.chung_lu(40000, 120000, 2.5, 1.0, 200.0, seed=21)
     roots = G.pick_roots(g.nv, 48, seed=21)
     rng = np.random.default_rng(21)
@@ -211,12 +222,13 @@ def test_wide_recompute_on_large_graph(sbc_lib):
     dg2.close()
 
 
-def test_bridge_deletions_in_one_call(sbc_lib, port_lib):
+@both_modes
+def test_bridge_deletions_in_one_call(sbc_lib, port_lib, mode):
     """Deletions in one call: roots whose deeper endpoint loses its last
-    parent leave the call's later deletions to a single recompute on the
-    final graph, while the other roots follow every deletion; chords first
-    keep most roots incremental, tree edges last send many roots to the
-    recompute.
+    parent move down, or (recompute mode) leave the call's later deletions to
+    a single recompute on the final graph, while the other roots follow every
+    deletion; chords first keep most roots incremental, tree edges last cut
+    many roots' trees.
     The state after the call equals the oracle's, deletion by deletion."""
     rng = np.random.default_rng(13)
     n = 400
@@ -242,6 +254,7 @@ def test_bridge_deletions_in_one_call(sbc_lib, port_lib):
     present = [bool(o.delete(int(u), int(v))) for u, v in dels]
     dg = native.DeviceGraph(g.nv, g.off, g.adj)
     f = native.DeviceForest(dg, roots)
+    f.set_delete_mode(mode)
     f.static_init()
     st = f.delete(dels)
     assert st["inserted"] == sum(present)
@@ -262,3 +275,108 @@ def test_bridge_deletions_in_one_call(sbc_lib, port_lib):
     _check(f, o)
     f.close()
     dg.close()
+
+
+def _two_halves(n_half, m_half, seed):
+    """Two ER halves joined by one edge between their largest-degree
+    vertices; returns the graph and that edge."""
+    a = G.er(n_half, m_half, seed=seed)
+    b = G.er(n_half, m_half, seed=seed + 1)
+    ea, eb = _edges(a), _edges(b) + n_half
+    bridge = (int(np.argmax(np.diff(a.off))), n_half + int(np.argmax(np.diff(b.off))))
+    e = np.concatenate([ea, eb, [bridge]])
+    return G.from_edges(2 * n_half, e[:, 0], e[:, 1]), bridge
+
+
+def test_move_down_deep_relevels_grid_and_cycle(sbc_lib, port_lib):
+    """A 24 x 24 grid (many shortest paths per vertex) joined to a cycle of
+    301: deletions move whole regions down by many levels, gaining and losing
+    parents on the way; every root's state after each deletion against the
+    oracle."""
+    w = 24
+    idx = np.arange(w * w).reshape(w, w)
+    grid = np.concatenate([np.stack([idx[:, :-1].ravel(), idx[:, 1:].ravel()], 1),
+                           np.stack([idx[:-1, :].ravel(), idx[1:, :].ravel()], 1)])
+    c0 = w * w
+    cyc = np.stack([c0 + np.arange(301), c0 + (np.arange(301) + 1) % 301], 1)
+    e = np.concatenate([grid, cyc, [[idx[w // 2, w // 2], c0]]])
+    n = c0 + 301
+    g = G.from_edges(n, np.minimum(e[:, 0], e[:, 1]), np.maximum(e[:, 0], e[:, 1]))
+    roots = np.unique(np.concatenate([G.pick_roots(n, 48, seed=31), [0, c0, c0 + 150, idx[w // 2, w // 2]]]))
+    rng = np.random.default_rng(31)
+    dels = np.concatenate([cyc[[0, 1, 150]], grid[rng.choice(len(grid), 30, replace=False)],
+                           [[idx[w // 2, w // 2], c0]]])
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.set_delete_mode(MOVE_DOWN)
+    f.static_init()
+    moved = 0
+    for u, v in dels:
+        u, v = int(min(u, v)), int(max(u, v))
+        assert o.delete(u, v)
+        st = f.delete([(u, v)])
+        moved += st["case2"]
+        _check(f, o)
+    assert moved > 0
+    f.close()
+    dg.close()
+
+
+def test_move_down_over_cap_recomputes_small_graph(sbc_lib, port_lib):
+    """Two ER halves of 1,200 vertices joined by one edge: deleting it leaves
+    each root's far half (more than the move-down cap of 1,024 vertices)
+    unreachable, so those roots are recomputed (a CTA per root) after the
+    call; deletions before and after it in the same call are followed."""
+    g, br = _two_halves(1200, 4800, seed=41)
+    roots = np.unique(np.concatenate([G.pick_roots(g.nv, 40, seed=41), list(br)]))
+    rng = np.random.default_rng(41)
+    edges = _edges(g)
+    other = edges[(edges[:, 0] != br[0]) | (edges[:, 1] != br[1])]
+    pick = other[rng.choice(len(other), 8, replace=False)]
+    dels = np.concatenate([pick[:4], [br], pick[4:]])
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, roots)
+    o.static()
+    for u, v in dels:
+        assert o.delete(int(u), int(v))
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.set_delete_mode(MOVE_DOWN)
+    f.static_init()
+    st = f.delete(dels)
+    assert st["inserted"] == len(dels) and st["case2"] > 0
+    _check(f, o)
+    f.close()
+    dg.close()
+
+
+def test_move_down_over_cap_recomputes_large_graph(sbc_lib):
+    """Two ER halves of 20,000 vertices joined by one edge (a graph of >= 32,768
+    vertices): the cut roots are recomputed with the whole GPU; the result
+    equals a static init of the graph without the edges."""
+    g, br = _two_halves(20000, 80000, seed=43)
+    roots = np.unique(np.concatenate([G.pick_roots(g.nv, 24, seed=43), list(br)]))
+    rng = np.random.default_rng(43)
+    edges = _edges(g)
+    other = edges[(edges[:, 0] != br[0]) | (edges[:, 1] != br[1])]
+    dels = np.concatenate([other[rng.choice(len(other), 6, replace=False)], [br]])
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    st = f.delete(dels)
+    assert st["inserted"] == len(dels) and st["case2"] > 0
+    keep = set(map(tuple, dels.tolist()))
+    e = np.asarray([(a, b) for a, b in edges.tolist() if (a, b) not in keep], dtype=np.int64)
+    g2 = G.from_edges(g.nv, e[:, 0], e[:, 1])
+    dg2 = native.DeviceGraph(g2.nv, g2.off, g2.adj)
+    f2 = native.DeviceForest(dg2, roots)
+    f2.static_init()
+    np.testing.assert_array_equal(f.dist(), f2.dist())
+    reach = f2.dist() != np.iinfo(np.int32).max
+    np.testing.assert_array_equal(f.sigma()[reach], f2.sigma()[reach])
+    assert_bc(f.bc(), f2.bc())
+    for x in (f, f2):
+        x.close()
+    dg.close()
+    dg2.close()
