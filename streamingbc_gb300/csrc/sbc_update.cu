@@ -398,6 +398,26 @@ cudaError_t launch_delete_finish(sbc_forest* f)
     return cudaMemsetAsync(f->d_dcnt, 0, sizeof(int), s);
 }
 
+// Launch shapes of k_delete_batch: the one with the forest's update shape's
+// threads per CTA (its worker scratch then fits: the grid is the forest's
+// worker count at most, and a CTA only indexes its own worker slot).
+template <int NT, int MINB, int ILP>
+void launch_delete_shape(const UpdateArgs& A, int grid, cudaStream_t s)
+{
+    k_delete_batch<NT, MINB, ILP><<<grid, NT, 0, s>>>(A);
+}
+
+struct DeleteShape {
+    int threads;
+    void (*launch)(const UpdateArgs&, int, cudaStream_t);
+};
+static const DeleteShape kDeleteShapes[] = {
+    {1024, launch_delete_shape<1024, 1, 8>},
+    {512, launch_delete_shape<512, 2, 4>},
+    {256, launch_delete_shape<256, 4, 4>},
+    {128, launch_delete_shape<128, 8, 2>},
+};
+
 cudaError_t launch_delete_batch(sbc_forest* f, int n)
 {
     sbc_graph* g = f->g;
@@ -425,7 +445,14 @@ cudaError_t launch_delete_batch(sbc_forest* f, int n)
     A.nwork = f->d_nwork;
     A.work_counter = f->d_counter;
     A.counters = f->d_counters;
-    k_delete_batch<512, 1, 4><<<(int)std::min<int64_t>(f->workers, f->nk), 512, 0, s>>>(A);
+    const int want = kVariants[f->variant].threads;
+    const DeleteShape* shape = &kDeleteShapes[3];
+    for (const DeleteShape& d : kDeleteShapes)
+        if (d.threads <= want) {
+            shape = &d;
+            break;
+        }
+    shape->launch(A, (int)std::min<int64_t>(f->workers, f->nk), s);
     return cudaGetLastError();
 }
 
