@@ -309,6 +309,23 @@ def insert_edges(g: Graph, ins: np.ndarray) -> Graph:
     return from_edges(g.nv, u, v)
 
 
+def delete_edges(g: Graph, dels: np.ndarray) -> Graph:
+    """Graph with the listed undirected edges removed (absent ones ignored)."""
+    src = np.repeat(np.arange(g.nv, dtype=np.int64), np.diff(g.off))
+    adj = g.adj.astype(np.int64)
+    d = np.asarray(dels, dtype=np.int64).reshape(-1, 2)
+    gone = np.concatenate([d[:, 0] * g.nv + d[:, 1], d[:, 1] * g.nv + d[:, 0]])
+    keep = ~np.isin(src * g.nv + adj, gone)
+    return from_edges(g.nv, src[keep], adj[keep])
+
+
+def edge_list(g: Graph) -> np.ndarray:
+    """Every undirected edge once, as (u, v) with u < v."""
+    src = np.repeat(np.arange(g.nv, dtype=np.int64), np.diff(g.off))
+    sel = src < g.adj
+    return np.stack([src[sel], g.adj[sel].astype(np.int64)], axis=1)
+
+
 # --------------------------------------------------------------------------
 # Named workloads (sizes as stated for each benchmark configuration).
 # --------------------------------------------------------------------------

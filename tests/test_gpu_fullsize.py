@@ -8,14 +8,17 @@ compare with the oracle (the reference COARSE path restated in C):
 * R-MAT scale 20, K = 1024 (the headline configuration): the benchmark's own
   path -- per-job cost logging over the first 16,384 insertions, cost-model
   training, the model schedule, the launch-shape tuner, then captured device
-  batches of 256 -- followed by a comparison of all 1024 roots with the
-  oracle's static recompute on the updated graph (incremental = static
-  recompute exactly, the reference's own property), 128 roots at a time.
+  batches of 256, then one call of 32 deletions (random edges, edges of
+  degree-1 vertices -- a move-down to unreachable on every root -- and edges
+  of a root) -- followed by a comparison of all 1024 roots with the oracle's
+  static recompute on the final graph (incremental = static recompute
+  exactly, the reference's own property), 128 roots at a time.
 * 64 R-MAT graphs of scales 10..16, K = min(|V|, 128), 512 insertions each,
   in tuned group batches of 16 per graph: every member against its own
   oracle recompute.
 * Chung-Lu n = 40,000, K = 256: all 4,096 insertions in captured device
-  batches of 64, against the incremental oracle every 512 insertions.
+  batches of 64, against the incremental oracle every 512 insertions, then
+  one call of 32 deletions (move-down) against the oracle.
 * Serving: the 8 smallest of the 16 configured serving graphs (K = 512),
   Poisson arrivals: every graph's state in the mix equals its state alone,
   and both equal the oracle recompute.
@@ -80,6 +83,19 @@ def test_rmat20_k1024_bench_path_vs_oracle(sbc_lib, port_lib):
         f.insert_device(B, du[s:].data_ptr(), dv[s:].data_ptr())
     f.sync()
     g2 = G.insert_edges(g, ins)
+    # deletions at full size, in one call
+    E = G.edge_list(g2)
+    rng = np.random.default_rng(29)
+    deg2 = np.diff(g2.off)
+    rows = f.dist(0, 8)
+    row0 = rows[np.argmax((rows != INF32).sum(axis=1))]  # a root in the giant component
+    leaf = E[((deg2[E[:, 0]] == 1) | (deg2[E[:, 1]] == 1)) & (row0[E[:, 0]] != INF32)]
+    at_root = E[(E[:, 0] == roots[0]) | (E[:, 1] == roots[0])]
+    dels = np.unique(np.concatenate([E[rng.choice(len(E), 24, replace=False)],
+                                     leaf[rng.choice(len(leaf), 6, replace=False)], at_root[:2]]), axis=0)
+    st = f.delete(dels)
+    assert st["inserted"] == len(dels) and st["case2"] >= 1024 and st["case1"] > 0
+    g2 = G.delete_edges(g2, dels)
     bc_ref = np.zeros(g.nv, dtype=np.float64)
     for r0 in range(0, len(roots), 128):
         bc_ref += _check_rows_vs_static(port_lib, g2, roots[r0:r0 + 128], f.dist(r0, 128), f.sigma(r0, 128))
@@ -148,6 +164,17 @@ def test_chunglu40k_all_insertions_captured_vs_oracle(sbc_lib, port_lib):
             assert_levels(f.level64(), lv)
             assert_sigma(f.sigma(), o.sigma(), lv)
             assert_bc(f.bc(), o.bc(), f"chunglu40k bc after {s + B} insertions")
+    g2 = G.insert_edges(g, ins)
+    E = G.edge_list(g2)
+    dels = E[np.random.default_rng(31).choice(len(E), 32, replace=False)]
+    st = f.delete(dels)
+    assert st["inserted"] == 32 and st["case2"] > 0
+    for u, v in dels:
+        assert o.delete(int(u), int(v))
+    lv = o.level()
+    assert_levels(f.level64(), lv)
+    assert_sigma(f.sigma(), o.sigma(), lv)
+    assert_bc(f.bc(), o.bc(), "chunglu40k bc after 32 deletions")
     o.close()
     f.close()
     dg.close()
