@@ -83,7 +83,7 @@ int ensure_staging(sbc_graph* g, int64_t n)
     if (g->h_ins) cudaFreeHost(g->h_ins);
     g->d_ins = nullptr;
     g->h_ins = nullptr;
-    CK(dev_alloc(&g->d_ins, (size_t)3 * cap));
+    CK(dev_alloc(&g->d_ins, (size_t)5 * cap + 1));  // u, v, codes, two rank rows and a flag (launch_append)
     CK(cudaMallocHost((void**)&g->h_ins, sizeof(int32_t) * 3 * (size_t)cap));
     g->ins_capacity = cap;
     return SBC_OK;
@@ -1621,6 +1621,8 @@ int sbc_group_create(sbc_group** out, int n, sbc_forest* const* forests, int var
         (e = cudaEventCreateWithFlags(&G->ev, cudaEventDisableTiming)) || (e = cudaEventCreate(&G->t0)) ||
         (e = cudaEventCreate(&G->t1)) || (e = dev_alloc(&G->d_worklist, (size_t)total)) ||
         (e = dev_alloc(&G->d_nwork, 2)) || (e = dev_alloc(&G->d_counters, SBC_NCOUNTERS)) ||
+        (e = dev_alloc(&G->d_errs, sbc::kMaxGroup)) ||
+        (e = cudaMallocHost((void**)&G->h_errs, sizeof(int) * sbc::kMaxGroup)) ||
         (e = cudaMemsetAsync(G->d_counters, 0, sizeof(unsigned long long) * SBC_NCOUNTERS, G->stream))) {
         sbc_group_destroy(G);
         return cuda_fail(e, "sbc_group_create");
@@ -1647,6 +1649,8 @@ int sbc_group_destroy(sbc_group* G)
     dev_free(G->d_worklist);
     dev_free(G->d_nwork);
     dev_free(G->d_counters);
+    dev_free(G->d_errs);
+    if (G->h_errs) cudaFreeHost(G->h_errs);
     if (G->ev) cudaEventDestroy(G->ev);
     if (G->t0) cudaEventDestroy(G->t0);
     if (G->t1) cudaEventDestroy(G->t1);
@@ -1720,9 +1724,13 @@ int sbc_group_insert_batch(sbc_group* G, const int64_t* counts, const int64_t* u
     std::vector<int> cs;
     if ((rc = group_stage(G, counts, u, v, cs))) return rc;
     if ((rc = group_after_members(G))) return rc;
+    const int ns = (int)G->members.size();
+    CK(cudaMemsetAsync(G->d_errs, 0, sizeof(int) * ns, G->stream));
     CK(cudaEventRecord(G->t0, G->stream));
     CK(sbc::launch_group_update(G, cs.data(), sbc::GROUP_ALL));
     CK(cudaEventRecord(G->t1, G->stream));
+    // every member's slack error flag, gathered by the seal: one copy
+    CK(cudaMemcpyAsync(G->h_errs, G->d_errs, sizeof(int) * ns, cudaMemcpyDeviceToHost, G->stream));
     if ((rc = members_after_group(G))) return rc;
     CK(cudaStreamSynchronize(G->stream));
     if (device_ms) {
@@ -1730,8 +1738,12 @@ int sbc_group_insert_batch(sbc_group* G, const int64_t* counts, const int64_t* u
         CK(cudaEventElapsedTime(&t, G->t0, G->t1));
         *device_ms = t;
     }
-    for (sbc_forest* f : G->members)
-        if ((rc = check_graph_err(f->g))) return rc;
+    for (int s = 0; s < ns; ++s)
+        if (G->h_errs[s]) {
+            sbc_graph* g = G->members[s]->g;
+            cudaMemsetAsync(g->d_err, 0, sizeof(int), g->stream);
+            return fail(SBC_ERR_STATE, "adjacency slack exhausted during an insertion batch (reserve capacity first)");
+        }
     return SBC_OK;
 }
 

@@ -68,6 +68,123 @@ __global__ void k_append(int64_t nv, const int64_t* __restrict__ row, int32_t* d
     append_warp(nv, row, deg, cap, col, seq, n, iu, iv, ok, directed, err);
 }
 
+// The same results with a warp per insertion, in three launches:
+//   k_append_codes  -1 bad id or loop; 0 an edge already (of the graph as the
+//                   batch begins -- sealed, so a binary search of the sorted
+//                   slots plus a scan of any tail -- or of an earlier
+//                   insertion of the batch); 1 to insert.
+//   k_append_rank   each insertion's rank among the batch's insertions at
+//                   each endpoint (its slot past deg0, so that every vertex's
+//                   appended slots stay in insertion order), and whether
+//                   every slot fits the vertex's slack.
+//   k_append_place  the slots written (seq = index) and the degrees raised;
+//                   if some slot does not fit, one warp appends the whole
+//                   batch in order instead (k_append's way), so that exactly
+//                   the insertions a one-by-one append rejects are rejected.
+// rk holds 2 n ranks and, at rk[2 n], the misfit flag.
+__global__ void k_append_codes(int64_t nv, const int64_t* __restrict__ row, const int32_t* __restrict__ deg,
+                               const int32_t* __restrict__ nsort, const int32_t* __restrict__ col, int n,
+                               const int32_t* __restrict__ iu, const int32_t* __restrict__ iv, int32_t* ok,
+                               int directed, int32_t* rk)
+{
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w == 0 && lane == 0) rk[2 * n] = 0;
+    if (w >= n) return;
+    const int u = iu[w], v = iv[w];
+    int code = (u == v || u < 0 || v < 0 || u >= nv || v >= nv) ? -1 : 1;
+    if (code == 1) {
+        bool dup = false;
+        for (int base = 0; base < w && !dup; base += 32) {
+            const int j = base + lane;
+            bool same = false;
+            if (j < w) {
+                const int a = iu[j], b = iv[j];
+                same = (a == u && b == v) || (!directed && a == v && b == u);
+            }
+            dup = __any_sync(0xffffffffu, same);
+        }
+        if (dup) code = 0;
+    }
+    if (code == 1) {
+        int x = u, y = v;
+        if (!directed && deg[v] < deg[u]) {
+            x = v;
+            y = u;
+        }
+        const int64_t rx = row[x];
+        const int d = deg[x], ns = min(nsort[x], d);
+        bool found = false;
+        if (lane == 0) {
+            int lo = 0, hi = ns;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                const int c = col[rx + mid];
+                if (c < y) lo = mid + 1;
+                else if (c > y) hi = mid;
+                else {
+                    found = true;
+                    break;
+                }
+            }
+        }
+        for (int s = ns + lane; s < d; s += 32)
+            if (col[rx + s] == y) found = true;
+        if (__any_sync(0xffffffffu, found)) code = 0;
+    }
+    if (lane == 0) ok[w] = code;
+}
+
+__global__ void k_append_rank(const int32_t* __restrict__ deg0, const int32_t* __restrict__ cap, int n,
+                              const int32_t* __restrict__ iu, const int32_t* __restrict__ iv,
+                              const int32_t* __restrict__ ok, int directed, int32_t* rk)
+{
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n || ok[w] != 1) return;
+    const int u = iu[w], v = iv[w];
+    int ru = 0, rv = 0;
+    for (int j = lane; j < w; j += 32) {
+        if (ok[j] != 1) continue;
+        const int a = iu[j], b = iv[j];
+        ru += (a == u || (!directed && b == u)) ? 1 : 0;
+        rv += (a == v || b == v) ? 1 : 0;
+    }
+    ru = __reduce_add_sync(0xffffffffu, ru);
+    rv = __reduce_add_sync(0xffffffffu, rv);
+    if (lane == 0) {
+        rk[w] = ru;
+        rk[n + w] = rv;
+        if (deg0[u] + ru >= cap[u] || (!directed && deg0[v] + rv >= cap[v])) atomicOr(&rk[2 * n], 1);
+    }
+}
+
+__global__ void k_append_place(int64_t nv, const int64_t* __restrict__ row, int32_t* deg,
+                               const int32_t* __restrict__ deg0, const int32_t* __restrict__ cap, int32_t* col,
+                               int32_t* seq, int n, const int32_t* __restrict__ iu, const int32_t* __restrict__ iv,
+                               int32_t* ok, int directed, const int32_t* __restrict__ rk, int* err)
+{
+    if (rk[2 * n]) {
+        // a slot does not fit: the whole batch in order, one warp
+        if (blockIdx.x == 0 && threadIdx.x < 32)
+            append_warp(nv, row, deg, cap, col, seq, n, iu, iv, ok, directed, err);
+        return;
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || ok[i] != 1) return;
+    const int u = iu[i], v = iv[i];
+    const int pu = deg0[u] + rk[i];
+    col[row[u] + pu] = v;
+    seq[row[u] + pu] = i;
+    atomicMax(&deg[u], pu + 1);
+    if (!directed) {
+        const int pv = deg0[v] + rk[n + i];
+        col[row[v] + pv] = u;
+        seq[row[v] + pv] = i;
+        atomicMax(&deg[v], pv + 1);
+    }
+}
+
 // Many graphs' batches at once: one warp (CTA) per graph, each appending its
 // graph's insertions in order exactly as k_append does.
 __global__ void k_append_group(const __grid_constant__ GraphBatchSlots S)
@@ -391,6 +508,7 @@ __global__ void __launch_bounds__(256) k_compact_removed(const int64_t* __restri
 __global__ void k_seal_group(const __grid_constant__ GraphBatchSlots S)
 {
     const GraphBatchSlot& b = S.slot[blockIdx.y];
+    if (S.errs && blockIdx.x == 0 && threadIdx.x == 0) S.errs[blockIdx.y] = *b.err;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= b.n || b.ok[i] <= 0) return;
     b.deg0[b.iu[i]] = b.deg[b.iu[i]];
@@ -419,9 +537,15 @@ cudaError_t launch_append(sbc_graph* g, int n, bool directed)
     const int32_t* iu = g->d_ins;
     const int32_t* iv = g->d_ins + g->ins_capacity;
     int32_t* ok = g->d_ins + 2 * g->ins_capacity;
-    k_append<<<1, 32, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_cap, g->d_col, g->d_seq, n, iu, iv, ok,
-                                      directed ? 1 : 0, g->d_err);
     g->last_directed = directed;
+    if (n <= 0) return cudaSuccess;
+    int32_t* rk = g->d_ins + 3 * g->ins_capacity;
+    const int wblocks = (n + 7) / 8;  // 8 warps of 32 per block, a warp per insertion
+    k_append_codes<<<wblocks, 256, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_nsort, g->d_col, n, iu, iv, ok,
+                                                   directed ? 1 : 0, rk);
+    k_append_rank<<<wblocks, 256, 0, g->stream>>>(g->d_deg0, g->d_cap, n, iu, iv, ok, directed ? 1 : 0, rk);
+    k_append_place<<<(n + 255) / 256, 256, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_deg0, g->d_cap, g->d_col,
+                                                           g->d_seq, n, iu, iv, ok, directed ? 1 : 0, rk, g->d_err);
     return cudaGetLastError();
 }
 

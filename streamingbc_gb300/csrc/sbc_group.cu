@@ -126,6 +126,7 @@ cudaError_t launch_group_update(sbc_group* G, const int* counts, unsigned steps)
     const int ns = (int)G->members.size();
     GraphBatchSlots B;
     B.count = ns;
+    B.errs = G->d_errs;
     GroupUpdateArgs A;
     A.nslots = ns;
     A.root_base[0] = 0;

@@ -139,7 +139,7 @@ struct sbc_graph {
     std::vector<int64_t> h_deg_ub;  // upper bound of the live degree
     // staging for insertion batches
     int ins_capacity = 0;
-    int32_t* d_ins = nullptr;  // [3 * ins_capacity]: u, v, ok
+    int32_t* d_ins = nullptr;  // [5 * ins_capacity + 1]: u, v, ok, then the append's ranks and misfit flag
     int32_t* h_ins = nullptr;  // pinned [3 * ins_capacity]
     cudaEvent_t staged = nullptr;  // recorded after the last copy out of h_ins
     const int32_t** d_src = nullptr;  // device slot: addresses of the caller's endpoint arrays
@@ -316,6 +316,8 @@ struct sbc_group {
     cudaEvent_t t0 = nullptr, t1 = nullptr;    // device time of the last batch
     double* h_bc = nullptr;                    // pinned staging of every member's BC
     int64_t h_bc_cap = 0;
+    int* d_errs = nullptr;  // [kMaxGroup]: each slot's slack error flag after a batch (the seal gathers them)
+    int* h_errs = nullptr;  // pinned copy
 };
 
 namespace sbc {
@@ -341,6 +343,7 @@ struct GraphBatchSlot {
 struct GraphBatchSlots {
     GraphBatchSlot slot[kMaxGroup];
     int count;
+    int* errs = nullptr;  // when set, the seal copies slot s's error flag to errs[s]
 };
 GraphBatchSlot graph_batch_slot(sbc_graph* g, int n);
 cudaError_t launch_append_group(const GraphBatchSlots& S, cudaStream_t s);
