@@ -435,8 +435,11 @@ __device__ __forceinline__ void ascend(const ForestSlot& A, UpdSmem<NT>& sm, con
                             const int q = __ffs(m) - 1;
                             m &= m - 1;
                             const int y = C1[q];
-                            const bool yDown = (W.st[y] & SBC_STEP_MASK) != 0;
-                            if (!yDown) {
+                            const int sy = W.st[y];
+                            const bool yDown = (sy & SBC_STEP_MASK) != 0;
+                            // a root neighbour is claimed by the first of its
+                            // many children; the others see the flag already
+                            if (!yDown && !(sy & SBC_ASC)) {
                                 const int old = atomicOr(&W.st[y], SBC_ASC);
                                 warp_append(&sm.at, W.qa, y, !(old & SBC_ASC));
                             }
