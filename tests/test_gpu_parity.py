@@ -511,3 +511,40 @@ def test_level2_masks_follow_graph_changes(sbc_lib, port_lib):
             else:
                 f.insert(edges)
         check_state(f, o.level(), o.sigma(), o.bc())
+
+
+def test_device_batch_without_slack_appends_in_order(sbc_lib, port_lib):
+    """Device batch (no host capacity planning, nothing reserved) that runs a
+    vertex out of slack: the parallel append falls back to the in-order append,
+    so the insertions at that vertex are taken in order until its slack ends
+    and the later ones are refused (the next sync reports it); the state is
+    that of the graph actually built, as a static recompute of it gives."""
+    torch = pytest.importorskip("torch")
+    g = G.er(300, 900, seed=8)
+    roots = G.pick_roots(g.nv, 60, seed=8)
+    hub = int(np.argmax(np.diff(g.off)))
+    nbr = set(g.adj[g.off[hub]:g.off[hub + 1]].tolist()) | {hub}
+    fresh = [x for x in range(g.nv) if x not in nbr][:40]
+    ins = np.array([(hub, x) for x in fresh], dtype=np.int64)
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    d = torch.tensor(ins, dtype=torch.int32, device="cuda")
+    du, dv = d[:, 0].contiguous(), d[:, 1].contiguous()
+    f.insert_device(len(ins), du.data_ptr(), dv.data_ptr())
+    with pytest.raises(native.SbcError):
+        f.sync()
+    off, adj = dg.to_csr()
+    got = set(adj[off[hub]:off[hub + 1]].tolist())
+    taken = [x for x in fresh if x in got]
+    assert 0 < len(taken) < len(fresh)
+    assert taken == fresh[:len(taken)]  # in insertion order, none skipped
+    g2 = G.from_edges(g.nv, np.repeat(np.arange(g.nv), np.diff(off)), adj)
+    o = port_lib.PortOracle(g2.nv, g2.off, g2.adj, roots)
+    o.static()
+    assert_levels(f.level64(), o.level())
+    assert_sigma(f.sigma(), o.sigma(), o.level())
+    assert_bc(f.bc(), o.bc())
+    o.close()
+    f.close()
+    dg.close()
