@@ -66,8 +66,8 @@ class ShardedForest:
     """One rank's share of a root-sharded forest.
 
     make_forest(roots) builds this rank's forest over its own copy of the
-    graph and runs the static init; insertions go to every rank in the same
-    order; bc() reduces the partial BC vectors over the group."""
+    graph and runs the static init; insertions and deletions go to every rank
+    in the same order; bc() reduces the partial BC vectors over the group."""
 
     def __init__(self, roots, rank: int, world: int, make_forest, group=None):
         self.rank, self.world, self.group = rank, world, group
@@ -78,6 +78,11 @@ class ShardedForest:
     def insert(self, pairs):
         """Apply a batch of insertions (the same batch on every rank)."""
         return self.forest.insert(pairs)
+
+    def delete(self, pairs):
+        """Apply a batch of edge deletions, in order (the same batch on every
+        rank; each rank's graph copy loses the edges, its roots are updated)."""
+        return self.forest.delete(pairs)
 
     def partial_bc(self) -> np.ndarray:
         return np.asarray(self.forest.bc(), dtype=np.float64)

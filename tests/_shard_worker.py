@@ -26,6 +26,10 @@ class OracleForest:
         for u, v in np.asarray(pairs).reshape(-1, 2):
             self.o.insert(int(u), int(v))
 
+    def delete(self, pairs):
+        for u, v in np.asarray(pairs).reshape(-1, 2):
+            self.o.delete(int(u), int(v))
+
     def bc(self):
         return self.o.bc()
 
@@ -45,6 +49,14 @@ def case(name):
     return g, G.pick_roots(g.nv, 300, seed=22), G.uniform_insertions(g, 40, seed=22)
 
 
+def deletions(name):
+    """Edges of the original graph removed after the insertions."""
+    from streamingbc_gb300 import graphs as G
+    g, _, _ = case(name)
+    E = G.edge_list(g)
+    return E[np.random.default_rng(23).choice(len(E), 12, replace=False)]
+
+
 def run(rank, world, port, name, out_dir, fail_rank=-1):
     import torch.distributed as dist
     from streamingbc_gb300.sharding import ShardedForest
@@ -56,6 +68,7 @@ def run(rank, world, port, name, out_dir, fail_rank=-1):
         sf = ShardedForest(roots, rank, world, lambda r: OracleForest(g, r))
         for s in range(0, len(ins), 16):
             sf.insert(ins[s:s + 16])
+        sf.delete(deletions(name))
         bc = sf.bc()
         lv = sf.level64()
         sg = sf.sigma()

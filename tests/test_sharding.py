@@ -1,6 +1,7 @@
 """Root sharding over processes (CPU, gloo): a forest split by roots across
 ranks, with the graph replicated and one BC reduce, ends in the state of the
-unsharded forest (levels/sigma exact, BC within 1e-9 relative)."""
+unsharded forest after insertions and deletions (levels/sigma exact, BC within
+1e-9 relative)."""
 from __future__ import annotations
 
 import os
@@ -41,6 +42,7 @@ def test_two_rank_sharded_forest_equals_unsharded(port_lib, tmp_path, name):
     g, roots, ins = W.case(name)
     ref = W.OracleForest(g, roots)
     ref.insert(ins)
+    ref.delete(W.deletions(name))
     assert_levels(z["lv"], ref.level64())
     assert_sigma(z["sg"], ref.sigma(), ref.level64())
     assert_bc(z["bc"], ref.bc())
