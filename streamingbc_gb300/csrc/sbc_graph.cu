@@ -459,8 +459,11 @@ __global__ void k_mark_removed(const int64_t* __restrict__ row, const int32_t* _
 }
 
 // Batched deletions, step 3 (after the update): the marked slots leave their
-// lists, which keep their order.  CTA per deletion endpoint; an endpoint that
-// an earlier removed deletion also names is left to that deletion's CTA.
+// lists, which keep their order.  CTA per deletion endpoint; the first CTA to
+// reach a vertex claims it by swapping its deg0 (== deg between batches) for
+// -1 until it is done, and CTAs that find it claimed leave it (one arriving
+// after the claimer finished compacts a clean list again, which changes
+// nothing).
 __global__ void __launch_bounds__(256) k_compact_removed(const int64_t* __restrict__ row, int32_t* deg, int32_t* deg0,
                                                          int32_t* nsort, int32_t* col, int32_t* seq, int n,
                                                          const int32_t* __restrict__ iu,
@@ -469,11 +472,16 @@ __global__ void __launch_bounds__(256) k_compact_removed(const int64_t* __restri
 {
     __shared__ int s_warp[8];
     __shared__ int s_keep_sorted;
+    __shared__ int s_mine;
     const int i = blockIdx.x >> 1;
     if (code[i] != 1) return;
     const int x = (blockIdx.x & 1) ? iv[i] : iu[i];
-    for (int j = 0; j < i; ++j)
-        if (code[j] == 1 && (iu[j] == x || iv[j] == x)) return;
+    if (threadIdx.x == 0) {
+        const int d0 = deg0[x];
+        s_mine = d0 >= 0 && atomicCAS(&deg0[x], d0, -1) == d0;
+    }
+    __syncthreads();
+    if (!s_mine) return;
     const int64_t rx = row[x];
     const int d = deg[x], ns = min(nsort[x], d);
     if (threadIdx.x == 0) s_keep_sorted = 0;
@@ -539,6 +547,12 @@ cudaError_t launch_append(sbc_graph* g, int n, bool directed)
     int32_t* ok = g->d_ins + 2 * g->ins_capacity;
     g->last_directed = directed;
     if (n <= 0) return cudaSuccess;
+    if (n > kParallelAppendMax) {
+        // the parallel form's within-batch tests grow with n^2
+        k_append<<<1, 32, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_cap, g->d_col, g->d_seq, n, iu, iv, ok,
+                                          directed ? 1 : 0, g->d_err);
+        return cudaGetLastError();
+    }
     int32_t* rk = g->d_ins + 3 * g->ins_capacity;
     const int wblocks = (n + 7) / 8;  // 8 warps of 32 per block, a warp per insertion
     k_append_codes<<<wblocks, 256, 0, g->stream>>>(g->nv, g->d_row, g->d_deg, g->d_nsort, g->d_col, n, iu, iv, ok,

@@ -451,6 +451,8 @@ cudaError_t launch_l2mask_remove_batch(sbc_graph* g, int n);
 // (codes into the staging's third row), and after the update the compaction
 // of the marked slots (and the masks' upkeep).
 cudaError_t launch_mark_removed(sbc_graph* g, int n);
+// Largest batch appended a warp per insertion (larger ones: one warp in order).
+constexpr int kParallelAppendMax = 8192;
 cudaError_t launch_compact_removed(sbc_graph* g, int n);
 cudaError_t launch_roster_build_list(sbc_forest* f, const int* d_list, const int* d_nlist);
 // Cost model and schedule (sbc_model.cu).

@@ -548,3 +548,33 @@ def test_device_batch_without_slack_appends_in_order(sbc_lib, port_lib):
     o.close()
     f.close()
     dg.close()
+
+
+def test_large_batch_in_order_append(sbc_lib, port_lib):
+    """A batch larger than the parallel append takes (10,000 insertions, with
+    repeats inside the batch and edges already present): appended in order by
+    one warp; the result equals a static recompute of the graph with the new
+    edges, and the counts split into inserted / duplicate as one-by-one
+    appends would."""
+    g = G.er(3000, 9000, seed=12)
+    roots = G.pick_roots(g.nv, 64, seed=12)
+    rng = np.random.default_rng(12)
+    new = rng.integers(0, g.nv, size=(9000, 2))
+    new = new[new[:, 0] != new[:, 1]]
+    E = G.edge_list(g)
+    ins = np.concatenate([new, new[:500, ::-1], E[:500]])[:10000]
+    rng.shuffle(ins)
+    dg = native.DeviceGraph(g.nv, g.off, g.adj)
+    f = native.DeviceForest(dg, roots)
+    f.static_init()
+    st = f.insert(ins)
+    g2 = G.insert_edges(g, ins)
+    assert st["inserted"] == g2.ne - g.ne and st["inserted"] + st["duplicates"] == len(ins)
+    o = port_lib.PortOracle(g2.nv, g2.off, g2.adj, roots)
+    o.static()
+    assert_levels(f.level64(), o.level())
+    assert_sigma(f.sigma(), o.sigma(), o.level())
+    assert_bc(f.bc(), o.bc())
+    o.close()
+    f.close()
+    dg.close()
