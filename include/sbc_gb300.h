@@ -369,6 +369,8 @@ int sbc_server_get_stats(sbc_server *s, sbc_server_stats *stats, int reset);
 #define SBC_DELETE_AUTO 0
 #define SBC_DELETE_MOVE_DOWN 1
 #define SBC_DELETE_RECOMPUTE 2
+/* A setting of the forest object (a new or restored forest starts in
+ * SBC_DELETE_AUTO); it applies to the deletions issued after the call. */
 int sbc_forest_set_delete_mode(sbc_forest *f, int mode);
 /* Remove n undirected edges in order, with the update of every root after
  * each, as n single deletions would.  One update launch serves the whole
