@@ -180,3 +180,27 @@ def test_pick_roots():
     assert np.unique(r).size == 100 and r.min() >= 0 and r.max() < 1000
     with pytest.raises(ValueError):
         G.pick_roots(5, 6, 0)
+
+
+def test_oracle_after_deletions_is_twice_networkx(port_lib):
+    """Independent check of the deletion oracle: exact BC (all roots) after
+    deletions that also cut vertices off equals 2 x networkx's betweenness of
+    the modified graph."""
+    nx = pytest.importorskip("networkx")
+    g = G.er(120, 260, seed=9)
+    E = G.edge_list(g)
+    deg = np.diff(g.off)
+    leaf = E[(deg[E[:, 0]] == 1) | (deg[E[:, 1]] == 1)][:3]
+    dels = np.concatenate([E[np.random.default_rng(9).choice(len(E), 12, replace=False)], leaf])
+    dels = np.unique(dels, axis=0)
+    o = port_lib.PortOracle(g.nv, g.off, g.adj, np.arange(g.nv))
+    o.static()
+    for u, v in dels:
+        assert o.delete(int(u), int(v))
+    h = nx.Graph()
+    h.add_nodes_from(range(g.nv))
+    keep = set(map(tuple, E.tolist())) - set(map(tuple, dels.tolist()))
+    h.add_edges_from(keep)
+    ref = nx.betweenness_centrality(h, normalized=False)
+    assert_bc(o.bc(), 2.0 * np.array([ref[i] for i in range(g.nv)]))
+    o.close()
